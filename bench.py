@@ -1,0 +1,365 @@
+#!/usr/bin/env python
+"""Benchmark of the BICOS matching path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload: the production stack, 1936x1216 uint8, n=33, limited descriptors
+(126 bits -> 128-bit words), nxcorr_threshold 0.96, min_variance 2.0,
+subpixel step 0.1, NoDuplicates; precision single (headline) and double.
+Seeded synthetic scenes (libbicos_gb300.scenes) stand in for the
+reference's dataset.  A step is one full match of one stereo stack.
+
+`value` is whole-job stereo Mpx/s with inputs resident in HBM; `e2e` is the
+same metric through the host-buffer C-ABI call (bicos_match_host_v1, what
+pybicos.match uses) with the H2D upload of both stacks and the D2H download
+of disparity + corrmap inside the timed region.  Under torchrun each rank
+matches its own stack (weak scaling, no collective on the data path).
+
+--impl reference times the reference's CPU implementation of the path on
+the host cores (the reference CPU backend compiled from source where the
+sources exist, else the project's C restatement of it), on a bounded sample
+of rows of the same workload per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = "mv1936_n33"
+METRIC = "stereo Mpx/s"
+THRESHOLD, MIN_VAR, STEP = 0.96, 2.0, 0.1
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-double", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target CPU work of the baseline sample")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0")), ws
+
+
+def workload_config(double=False):
+    return {"workload": f"{WORKLOAD}: 1936x1216 uint8 stereo stack, n=33, limited descriptors (128-bit), "
+                        f"threshold {THRESHOLD}, min_variance {MIN_VAR}, subpixel step {STEP}, NoDuplicates, "
+                        f"precision {'double' if double else 'single'}",
+            "rows": 1216, "cols": 1936, "n": 33, "input": "uint8",
+            "l2": "inputs larger than L2: 155 MB of frames streamed per step (L2 129 MB)"}
+
+
+def oracle_mpx(scene, rows, cfg, use_ref=False, nthreads=0):
+    from oracle import oracle as O
+    t = time.perf_counter()
+    O.match(scene.left[:, :rows], scene.right[:, :rows], cfg, nthreads=nthreads, use_ref=use_ref)
+    dt = time.perf_counter() - t
+    return rows * scene.left.shape[2] / dt / 1e6, dt
+
+
+def cpu_sample_rows(scene, cfg, target_s, use_ref=False):
+    probe = 8
+    _, dt = oracle_mpx(scene, probe, cfg, use_ref)
+    return int(max(probe, min(scene.left.shape[1], target_s / max(dt / probe, 1e-6))))
+
+
+def cpu_baseline(scene, target_s):
+    from oracle import oracle as O
+    cfg = O.make_config(threshold=THRESHOLD, step=STEP, min_variance=MIN_VAR)
+    use_ref = O.ref_available()
+    rows = cpu_sample_rows(scene, cfg, target_s, use_ref)
+    mpx, dt = oracle_mpx(scene, rows, cfg, use_ref)
+    return {"value": round(mpx, 4), "unit": METRIC, "cores": O.lib().orc_num_threads(0) if not use_ref else os.cpu_count(),
+            "kind": "reference" if use_ref else "port",
+            "sample": f"rows 0..{rows - 1} of the {WORKLOAD} stack (all 1936 columns, n=33), {dt:.1f} s"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.proc = None
+        self.lines = []
+        self.dev = device_index
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return p["hbm_gbs"], p["bf16_tflops"], "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, 1900.0, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per launch of the search kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "search_mv1936_n33.md")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    rank, local_rank, ws = dist_env()
+    if ws > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local_rank)
+    device = torch.device("cuda", local_rank)
+
+    import libbicos_gb300 as lbg
+    from libbicos_gb300 import _native as N
+    from libbicos_gb300 import build as B
+    from libbicos_gb300 import pybicos, scenes
+    import ctypes as C
+
+    B.build()
+    L = lbg.load_library()
+    scene = scenes.workload_scene(WORKLOAD, seed=args.seed + rank)
+    n, rows, cols = scene.left.shape
+    px = rows * cols
+    left = torch.from_numpy(scene.left).to(device)
+    right = torch.from_numpy(scene.right).to(device)
+
+    def cfg_of(double):
+        c = pybicos.Config()
+        c.nxcorr_threshold, c.min_variance, c.subpixel_step = THRESHOLD, MIN_VAR, STEP
+        c.precision = pybicos.Double if double else pybicos.Single
+        return c
+
+    def barrier():
+        if ws > 1:
+            dist.barrier()
+
+    def max_over_ranks(v):
+        if ws == 1:
+            return v
+        t = torch.tensor([v], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def timed(double, steps, warmup, stage_times=False):
+        cfg = cfg_of(double)
+        out = lbg.match_device(left, right, cfg)
+        for _ in range(warmup):
+            lbg.match_device(left, right, cfg, out=out)
+        stream = torch.cuda.current_stream()
+        if stage_times:
+            N.check(L.bicos_stage_timing(1))
+        barrier()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            lbg.match_device(left, right, cfg, out=out)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        ms = e0.elapsed_time(e1) / steps
+        st = None
+        if stage_times:
+            arr = (C.c_float * 3)()
+            calls = C.c_int32()
+            N.check(L.bicos_stage_times(arr, C.byref(calls)))
+            N.check(L.bicos_stage_timing(0))
+            st = [arr[i] / max(calls.value, 1) for i in range(3)]
+        return max_over_ranks(ms), st, out
+
+    dev_index = torch.cuda.current_device()
+    try:
+        uuid = str(torch.cuda.get_device_properties(dev_index).uuid)
+        smi_dev = uuid if uuid.startswith("GPU-") else f"GPU-{uuid}"
+    except Exception:
+        smi_dev = dev_index
+    with ClockSampler(smi_dev) as clocks:
+        ms, stages, out = timed(False, args.steps, args.warmup, stage_times=True)
+    clk = clocks.summary()
+    value = ws * px / (ms * 1e-3) / 1e6
+
+    valid = float(torch.isfinite(out[0]).float().mean().item())
+    result = {
+        "metric": METRIC, "value": round(value, 3), "unit": "Mpx/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u8", "data": f"synthetic (seeded scene, seed {args.seed}+rank)",
+        "config": dict(workload_config(False), parallelism=f"replicas x{ws}" if ws > 1 else "single GPU"),
+        "valid_fraction": round(valid, 4),
+    }
+    result["stage_ms"] = {"transform": round(stages[0], 4), "search": round(stages[1], 4),
+                          "agree_subpixel": round(stages[2], 4)}
+    result["gpu_launches"] = 3 * args.steps
+
+    # dominant kernel roofline: the Hamming search
+    hbm, tf, src = peaks()
+    nw = 4
+    search_ms = stages[1]
+    word_ops = rows * cols * cols * nw  # 32-bit XOR+POPC word-ops per launch
+    algo_bytes = 2 * px * nw * 4 + px * 2
+    sm_clock = clk["sm_mhz"] or 1900.0
+    popc_peak = 16 * 152 * sm_clock * 1e6 / 1e9  # POPC results/clk/SM x SMs x clock, Gop/s
+    achieved = word_ops / (search_ms * 1e-3) / 1e9
+    traffic = profile_traffic()
+    result["roofline"] = {
+        "kernel": "k_search (popcount Hamming arg-min)", "bound": "int-popc",
+        "achieved": round(achieved, 1), "peak": round(popc_peak, 1), "unit": "Gop/s",
+        "frac": round(achieved / popc_peak, 4),
+        "peak_source": f"16 POPC/clk/SM x 152 SMs x median SM clock {sm_clock:.0f} MHz",
+        "traffic": traffic, "algorithmic_bytes": algo_bytes,
+        "hbm_frac_of_" + src: round(algo_bytes / (search_ms * 1e-3) / 1e9 / hbm, 5),
+    }
+
+    if not args.no_double:
+        ms_d, st_d, _ = timed(True, max(1, args.steps // 2), 2, stage_times=True)
+        result["double"] = {"value": round(ws * px / (ms_d * 1e-3) / 1e6, 3), "unit": "Mpx/s",
+                            "ms_per_step": round(ms_d, 4),
+                            "stage_ms": {"transform": round(st_d[0], 4), "search": round(st_d[1], 4),
+                                         "agree_subpixel": round(st_d[2], 4)}}
+
+    if not args.no_e2e:
+        # host path: pinned host stacks -> bicos_match_host_v1 (upload, match, download)
+        cfg = cfg_of(False)
+        nc = cfg.native()
+        lh = torch.from_numpy(scene.left).pin_memory().numpy()
+        rh = torch.from_numpy(scene.right).pin_memory().numpy()
+        dh = torch.empty((rows, cols), dtype=torch.float32).pin_memory().numpy()
+        ch = torch.empty((rows, cols), dtype=torch.float32).pin_memory().numpy()
+        p0 = (C.c_void_p * n)(*[lh[t].ctypes.data for t in range(n)])
+        p1 = (C.c_void_p * n)(*[rh[t].ctypes.data for t in range(n)])
+        sptr = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+        def host_call():
+            N.check(L.bicos_match_host_v1(p0, p1, n, rows, cols, N.BICOS_8U, cols, dh.ctypes.data, cols * 4,
+                                          ch.ctypes.data, cols * 4, C.byref(nc), sptr))
+        for _ in range(2):
+            host_call()
+        k_e = max(3, min(args.steps, 20))
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(k_e):
+            host_call()
+        t_e = max_over_ranks((time.perf_counter() - t0) / k_e)
+        result["e2e"] = {"value": round(ws * px / t_e / 1e6, 3), "unit": "Mpx/s",
+                         "h2d_bytes_per_step": int(2 * n * px), "d2h_bytes_per_step": int(px * 8),
+                         "ms_per_step": round(t_e * 1e3, 3), "api": "bicos_match_host_v1 (pinned host buffers)"}
+
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        result["cpu_baseline"] = cpu_baseline(scene, args.cpu_seconds)
+    result["clocks"] = clk
+    if rank == 0:
+        print(json.dumps(result), flush=True)
+    if ws > 1:
+        dist.destroy_process_group()
+
+
+def run_reference(args):
+    rank, _, ws = dist_env()
+    if rank != 0:
+        return
+    from libbicos_gb300 import scenes
+    from oracle import oracle as O
+    O.build()
+    use_ref = O.ref_available()
+    scene = scenes.workload_scene(WORKLOAD, seed=args.seed)
+    cfg = O.make_config(threshold=THRESHOLD, step=STEP, min_variance=MIN_VAR)
+    # each step: a bounded sample of rows, ~1.5 s of CPU work
+    rows = cpu_sample_rows(scene, cfg, 1.5, use_ref)
+    for _ in range(args.warmup):
+        oracle_mpx(scene, rows, cfg, use_ref)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        oracle_mpx(scene, rows, cfg, use_ref)
+    dt = (time.perf_counter() - t0) / args.steps
+    value = rows * scene.left.shape[2] / dt / 1e6
+    cores = os.cpu_count() if use_ref else O.lib().orc_num_threads(0)
+    kind = "reference" if use_ref else "port"
+    sample = f"rows 0..{rows - 1} of the {WORKLOAD} stack (all columns, n=33) per step"
+    print(json.dumps({
+        "metric": METRIC, "value": round(value, 4), "unit": "Mpx/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(dt * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u8", "data": f"synthetic (seeded scene, seed {args.seed})",
+        "config": workload_config(False), "impl": "reference",
+        "cpu_baseline": {"value": round(value, 4), "unit": "Mpx/s", "cores": cores, "kind": kind, "sample": sample},
+        "e2e": {"value": round(value, 4), "unit": "Mpx/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,196 @@
+/*
+ * bicos_gb300 -- C ABI of the GB300-native BICOS matcher (sm_103a).
+ *
+ * This is the drop-in boundary for libBICOS's matching path.  Every entry
+ * point takes plain pointers, sizes and POD structs; images are device
+ * resident, one pitched 2-D image per frame, exactly as the reference's
+ * cv::cuda::GpuMat inputs.  Work is enqueued on the caller's stream and the
+ * call returns without waiting for it (the reference returned after its
+ * implicit synchronisation; call cudaStreamSynchronize to get that).
+ *
+ * Reference interfaces replaced (paths inside libBICOS 2.2.0):
+ *   bicos_match_v1                 BICOS::match, include/match.hpp:31-41,
+ *                                  src/lib.cpp:31-49, src/impl/cuda.cu.in:233-292
+ *   bicos_descriptor_transform_v1  transform_{limited,full}_kernel,
+ *                                  include/impl/cuda/descriptor_transform.cuh:30-149
+ *   bicos_search_v1                bicos_kernel(_smem),
+ *                                  include/impl/cuda/bicos.cuh:77-176
+ *   bicos_agree_v1                 agree_kernel, include/impl/cuda/agree.cuh:110-159
+ *   bicos_agree_subpixel_v1        agree_subpixel_kernel,
+ *                                  include/impl/cuda/agree.cuh:161-259
+ *   bicos_config_default           BICOS::Config defaults, include/common.hpp:73-82
+ *   bicos_last_error               BICOS::Exception::what(), src/exception.cpp:23-27
+ *
+ * Error behaviour: every entry point returns a bicos_status.  Messages match
+ * the reference's exception texts ("need at least two images", "bad input
+ * depths, only CV_8UC1 and CV_16UC1 are supported", "input stacks too large,
+ * would require N bits") and are read back with bicos_last_error(), which is
+ * per thread.  BICOS_ERR_INVALID_ARGUMENT corresponds to the reference's
+ * std::invalid_argument, BICOS_ERR_EXCEPTION to BICOS::Exception.
+ */
+#ifndef BICOS_GB300_C_H
+#define BICOS_GB300_C_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* a cudaStream_t; 0 is the legacy default stream */
+typedef struct CUstream_st* bicos_stream_t;
+
+/* element types: OpenCV's single-channel type codes (CV_8UC1 ...) */
+enum {
+    BICOS_8U = 0,
+    BICOS_16U = 2,
+    BICOS_16S = 3,
+    BICOS_32F = 5,
+    BICOS_64F = 6
+};
+
+typedef enum bicos_status {
+    BICOS_OK = 0,
+    BICOS_ERR_EXCEPTION = 1,        /* BICOS::Exception */
+    BICOS_ERR_INVALID_ARGUMENT = 2, /* std::invalid_argument */
+    BICOS_ERR_CUDA = 3              /* a CUDA runtime error (BICOS::Exception in the reference) */
+} bicos_status;
+
+/* a pitched device image (the layout of cv::cuda::GpuMat's header) */
+typedef struct bicos_image {
+    void* data;
+    size_t step; /* bytes between rows */
+    int32_t rows;
+    int32_t cols;
+    int32_t type; /* BICOS_8U ... */
+    int32_t reserved;
+} bicos_image;
+
+/* descriptor transform modes, BICOS::TransformMode */
+enum { BICOS_MODE_LIMITED = 0, BICOS_MODE_FULL = 1 };
+/* NCC precision, BICOS::Precision */
+enum { BICOS_PRECISION_SINGLE = 0, BICOS_PRECISION_DOUBLE = 1 };
+/* search variant, BICOS::Variant::{NoDuplicates, Consistency} */
+enum { BICOS_VARIANT_NODUPLICATES = 0, BICOS_VARIANT_CONSISTENCY = 1 };
+/* search flags, include/impl/common.hpp:46-47 */
+enum { BICOS_FLAG_NODUPES = 1, BICOS_FLAG_CONSISTENCY = 2 };
+
+/* BICOS::Config, field for field; std::optional<float> is (has_x, x) */
+typedef struct bicos_config {
+    int32_t has_threshold;
+    float nxcorr_threshold;   /* default 0.5 */
+    int32_t has_subpixel_step;
+    float subpixel_step;      /* default none */
+    int32_t has_min_variance;
+    float min_variance;       /* default none; per frame, scaled by n internally */
+    int32_t mode;             /* default BICOS_MODE_LIMITED */
+    int32_t precision;        /* default BICOS_PRECISION_SINGLE */
+    int32_t variant;          /* default BICOS_VARIANT_NODUPLICATES */
+    int32_t max_lr_diff;      /* Consistency only, default 1 */
+    int32_t no_dupes;         /* Consistency only, default 0 */
+    int32_t max_bits;         /* descriptor width limit: 256 as the reference;
+                                 up to 512 accepts FULL stacks of n <= 23 (extension) */
+} bicos_config;
+
+/* Fills the reference defaults (include/common.hpp:73-82). */
+bicos_status bicos_config_default(bicos_config* cfg);
+
+/* Per-thread text of the last error. */
+const char* bicos_last_error(void);
+
+/* Output element types match() produces for a configuration:
+ * disparity BICOS_16S (no threshold or no step) or BICOS_32F (step);
+ * corrmap BICOS_32F / BICOS_64F by precision, or -1 when none is made. */
+bicos_status bicos_output_types(const bicos_config* cfg, int32_t* disparity_type,
+                                int32_t* corrmap_type);
+
+/* Descriptor width in 32-bit words for n frames in a mode (1, 2, 4, 8; 12
+ * or 16 past 256 bits when max_bits allows), or -1 when too large. */
+int32_t bicos_descriptor_words(uint32_t n, int32_t mode, int32_t max_bits);
+
+/*
+ * The whole matching path: BICOS::match(stack0, stack1, disparity, cfg,
+ * corrmap, stream).
+ *   stack0, stack1  n device images each, all of one size and of type
+ *                   BICOS_8U or BICOS_16U
+ *   disparity       caller-allocated device image of the size of the stack
+ *                   and of the type bicos_output_types() reports
+ *   corrmap         NULL, or a device image likewise; pixels that get no
+ *                   correlation are NaN
+ * Scratch (descriptors, raw disparities) comes from a per-device cache that
+ * grows on demand and is reused across calls; calls on several streams are
+ * ordered by an event.  bicos_release_scratch() frees it.
+ */
+bicos_status bicos_match_v1(const bicos_image* stack0, const bicos_image* stack1, uint32_t n,
+                            bicos_image* disparity, bicos_image* corrmap,
+                            const bicos_config* cfg, bicos_stream_t stream);
+
+/*
+ * bicos_match_v1 over HOST buffers, synchronous: the path pybicos.match
+ * takes (src/pybicos.cpp:102-119 uploads each image, matches, downloads).
+ * frames0/frames1 are n host pointers to rows x cols images of `type` with
+ * row step host_step; disparity (and corrmap, may be NULL) are host buffers
+ * of the types bicos_output_types() reports.  Device copies live in a
+ * per-device staging cache; returns after the results are in host memory.
+ */
+bicos_status bicos_match_host_v1(const void* const* frames0, const void* const* frames1, uint32_t n,
+                                 int32_t rows, int32_t cols, int32_t type, size_t host_step,
+                                 void* disparity, size_t disparity_step, void* corrmap,
+                                 size_t corrmap_step, const bicos_config* cfg,
+                                 bicos_stream_t stream);
+
+/* Frees this device's cached scratch memory (waits for its last use). */
+bicos_status bicos_release_scratch(void);
+
+/*
+ * Stage entry points (kernel-level interfaces of the reference).
+ * Descriptors are dense [rows][cols][nwords] uint32 arrays in device
+ * memory, bit i of a descriptor in word i/32, bit i%32.
+ */
+bicos_status bicos_descriptor_transform_v1(const bicos_image* stack, uint32_t n, int32_t mode,
+                                           uint32_t nwords, uint32_t* descriptors,
+                                           bicos_stream_t stream);
+
+/* Row-wise Hamming arg-min of desc0 against desc1 with flags
+ * (BICOS_FLAG_*; 0 = plain first minimum).  Writes int16 disparities
+ * col0 - col1 (INT16_MIN = invalid) to `disparity` (BICOS_16S). */
+bicos_status bicos_search_v1(const uint32_t* desc0, const uint32_t* desc1, int32_t rows,
+                             int32_t cols, uint32_t nwords, int32_t flags, int32_t max_lr_diff,
+                             bicos_image* disparity, bicos_stream_t stream);
+
+/* NCC agreement in place on an int16 disparity; min_var is the per-stack
+ * threshold (min_variance * n) used when has_min_var is set. */
+bicos_status bicos_agree_v1(bicos_image* disparity, const bicos_image* stack0,
+                            const bicos_image* stack1, uint32_t n, float nxcorr_threshold,
+                            int32_t has_min_var, float min_var, int32_t precision,
+                            bicos_image* corrmap, bicos_stream_t stream);
+
+/* NCC agreement with the subpixel sweep x = -1, -1+step, ... <= 1 (float
+ * accumulated); writes a BICOS_32F disparity (NaN = invalid). */
+bicos_status bicos_agree_subpixel_v1(const bicos_image* raw_disparity, const bicos_image* stack0,
+                                     const bicos_image* stack1, uint32_t n,
+                                     float nxcorr_threshold, float subpixel_step,
+                                     int32_t has_min_var, float min_var, int32_t precision,
+                                     bicos_image* disparity, bicos_image* corrmap,
+                                     bicos_stream_t stream);
+
+/*
+ * Stage timing for measurement tools (no counterpart in the reference,
+ * whose CLI times whole calls with std::chrono, src/cli.cpp:188-194).  While
+ * enabled, each bicos_match_v1 call records CUDA events on its stream
+ * around its three stages (descriptor transform, search, agreement), for up
+ * to 1024 calls.  bicos_stage_times() waits for those events and returns the
+ * summed milliseconds per stage and the number of calls, then starts over.
+ */
+bicos_status bicos_stage_timing(int32_t enable);
+bicos_status bicos_stage_times(float* ms_per_stage /* [3] */, int32_t* calls);
+
+/* Library version string. */
+const char* bicos_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BICOS_GB300_C_H */

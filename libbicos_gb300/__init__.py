@@ -1,0 +1,146 @@
+"""bicos_gb300: GB300-native (sm_103a) BICOS stereo matching.
+
+The matching path of libBICOS -- binary temporal descriptor transform,
+row-wise Hamming arg-min with the no-duplicates / consistency postfilter,
+NCC agreement with optional subpixel sweep -- as hand-written CUDA kernels
+behind a C ABI (include/bicos_c.h), a C++ ``BICOS::match`` API
+(include/BICOS/) and the ``pybicos`` Python surface (``.pybicos``).
+
+Device-side helpers here take CUDA tensors (torch is only the container for
+device memory and streams); they call the C ABI directly with zero copies.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+from . import _native as N
+from . import pybicos
+from .pybicos import Config, Precision, TransformMode, Variant
+
+__all__ = ["pybicos", "Config", "Precision", "TransformMode", "Variant", "match_device",
+           "descriptor_transform", "search", "agree", "agree_subpixel", "descriptor_words",
+           "load_library", "required_bits"]
+
+
+def load_library():
+    """Load the native library; raises ImportError when it is not built."""
+    return N.load()
+
+
+def required_bits(n: int, full: bool) -> int:
+    return n * n - 2 * n + 3 if full else 4 * n - 7
+
+
+def descriptor_words(n: int, full: bool, max_bits: int = 256) -> int:
+    return N.load().bicos_descriptor_words(n, 1 if full else 0, max_bits)
+
+
+def _stream_ptr(stream):
+    import torch
+    s = torch.cuda.current_stream() if stream is None else stream
+    return C.c_void_p(s.cuda_stream)
+
+
+def _frames(stack):
+    """A (n, rows, cols) tensor or a sequence of 2-D tensors -> bicos_image[]."""
+    frames = [stack[i] for i in range(stack.shape[0])] if hasattr(stack, "dim") and stack.dim() == 3 else list(stack)
+    for f in frames:
+        if not f.is_cuda:
+            raise ValueError("device API expects CUDA tensors")
+    return N.image_array([N.tensor_image(f) for f in frames]), len(frames), frames[0]
+
+
+def _raise(st):
+    try:
+        N.check(st)
+    except N.NativeError as e:
+        pybicos.raise_native(e)
+
+
+def match_device(stack0, stack1, cfg: Config | None = None, stream=None, out=None, corrmap=True,
+                 max_bits: int = 256):
+    """BICOS::match on CUDA tensors.  Returns (disparity, corrmap or None).
+
+    stack0/stack1: (n, rows, cols) uint8/uint16 CUDA tensors or lists of
+    2-D ones.  ``out`` may supply (disparity, corrmap) tensors to reuse.
+    Enqueued on ``stream`` (torch's current stream by default); returns
+    without synchronising.
+    """
+    import torch
+    cfg = Config() if cfg is None else cfg
+    nc = cfg.native()
+    nc.max_bits = max_bits
+    a0, n, f0 = _frames(stack0)
+    a1, n1, _ = _frames(stack1)
+    if n1 != n:
+        raise pybicos.Exception("both stacks must hold the same number of images")
+    dt, ct = C.c_int32(), C.c_int32()
+    N.check(N.load().bicos_output_types(C.byref(nc), C.byref(dt), C.byref(ct)))
+    rows, cols = f0.shape
+    if out is not None:
+        disp, corr = out
+    else:
+        disp = torch.empty((rows, cols), dtype=torch.int16 if dt.value == N.BICOS_16S else torch.float32,
+                           device=f0.device)
+        corr = None
+        if corrmap and ct.value >= 0:
+            corr = torch.empty((rows, cols), dtype=torch.float64 if ct.value == N.BICOS_64F else torch.float32,
+                               device=f0.device)
+    di = N.tensor_image(disp)
+    ci = N.tensor_image(corr) if corr is not None else None
+    st = N.load().bicos_match_v1(a0, a1, n, C.byref(di), C.byref(ci) if ci is not None else None,
+                                 C.byref(nc), _stream_ptr(stream))
+    _raise(st)
+    return disp, corr
+
+
+def descriptor_transform(stack, full: bool, stream=None):
+    """Descriptors of one stack: (rows, cols, nwords) uint32 as int32 tensor."""
+    import torch
+    arr, n, f0 = _frames(stack)
+    nw = descriptor_words(n, full, 512)
+    if nw < 0:
+        raise ValueError(f"input stacks too large, would require {required_bits(n, full)} bits")
+    rows, cols = f0.shape
+    out = torch.empty((rows, cols, nw), dtype=torch.int32, device=f0.device)
+    _raise(N.load().bicos_descriptor_transform_v1(arr, n, 1 if full else 0, nw, C.c_void_p(out.data_ptr()),
+                                                  _stream_ptr(stream)))
+    return out
+
+
+def search(desc0, desc1, flags: int, max_lr_diff: int = -1, stream=None):
+    """Hamming arg-min of (rows, cols, nwords) descriptor tensors -> int16 disparity."""
+    import torch
+    rows, cols, nw = desc0.shape
+    out = torch.empty((rows, cols), dtype=torch.int16, device=desc0.device)
+    oi = N.tensor_image(out)
+    _raise(N.load().bicos_search_v1(C.c_void_p(desc0.data_ptr()), C.c_void_p(desc1.data_ptr()), rows, cols, nw,
+                                    flags, max_lr_diff, C.byref(oi), _stream_ptr(stream)))
+    return out
+
+
+def agree(disp, stack0, stack1, threshold: float, min_var=None, double=False, stream=None):
+    """In-place NCC agreement on an int16 disparity; returns (disp, corrmap).
+    min_var is the per-stack value (min_variance * n)."""
+    import torch
+    a0, n, f0 = _frames(stack0)
+    a1, _, _ = _frames(stack1)
+    corr = torch.empty(disp.shape, dtype=torch.float64 if double else torch.float32, device=disp.device)
+    di, ci = N.tensor_image(disp), N.tensor_image(corr)
+    _raise(N.load().bicos_agree_v1(C.byref(di), a0, a1, n, threshold, int(min_var is not None),
+                                   float(min_var or 0.0), int(double), C.byref(ci), _stream_ptr(stream)))
+    return disp, corr
+
+
+def agree_subpixel(raw, stack0, stack1, threshold: float, step: float, min_var=None, double=False, stream=None):
+    """NCC agreement with subpixel sweep; returns (float32 disparity, corrmap)."""
+    import torch
+    a0, n, f0 = _frames(stack0)
+    a1, _, _ = _frames(stack1)
+    out = torch.empty(raw.shape, dtype=torch.float32, device=raw.device)
+    corr = torch.empty(raw.shape, dtype=torch.float64 if double else torch.float32, device=raw.device)
+    ri, oi, ci = N.tensor_image(raw), N.tensor_image(out), N.tensor_image(corr)
+    _raise(N.load().bicos_agree_subpixel_v1(C.byref(ri), a0, a1, n, threshold, step, int(min_var is not None),
+                                            float(min_var or 0.0), int(double), C.byref(oi), C.byref(ci),
+                                            _stream_ptr(stream)))
+    return out, corr

@@ -1,0 +1,584 @@
+// C ABI and host orchestration of the matching path.
+//
+// Follows the control flow of libBICOS src/impl/cuda.cu.in:54-292 (input
+// validation, descriptor width dispatch, transform -> search -> agree), but
+// GB300-first: one stream (the caller's), no per-call cudaMalloc /
+// cudaHostRegister / stream or event creation, kernel parameters by value,
+// and the disparity output written by the kernels themselves (no fills).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "../../include/bicos_c.h"
+#include "kernels.cuh"
+
+using namespace bicos_gb300;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+bicos_status fail(bicos_status s, const std::string& msg) {
+    g_last_error = msg;
+    return s;
+}
+
+bicos_status cuda_fail(cudaError_t e, const char* where) {
+    return fail(BICOS_ERR_CUDA, std::string("libBICOS CUDA error in ") + where + ": " + cudaGetErrorString(e));
+}
+
+#define BICOS_CUDA_TRY(call)                       \
+    do {                                           \
+        cudaError_t e_ = (call);                   \
+        if (e_ != cudaSuccess)                     \
+            return cuda_fail(e_, #call);           \
+    } while (0)
+
+// ---- per-device scratch cache ------------------------------------------
+
+struct Scratch {
+    std::mutex mu;
+    void* buf = nullptr;
+    size_t cap = 0;
+    cudaEvent_t ev = nullptr;
+    cudaStream_t last = nullptr;
+    bool used = false;
+};
+
+constexpr int kMaxDevices = 64;
+Scratch g_scratch[kMaxDevices];
+Scratch g_staging[kMaxDevices];  // device copies of host inputs/outputs (bicos_match_host_v1)
+
+// Returns a buffer of >= bytes usable on `st`, ordered after its last use.
+cudaError_t scratch_acquire(Scratch& s, size_t bytes, cudaStream_t st, void** out) {
+    if (!s.ev) {
+        cudaError_t e = cudaEventCreateWithFlags(&s.ev, cudaEventDisableTiming);
+        if (e != cudaSuccess)
+            return e;
+    }
+    if (s.cap < bytes) {
+        if (s.used) {
+            cudaError_t e = cudaEventSynchronize(s.ev);
+            if (e != cudaSuccess)
+                return e;
+        }
+        if (s.buf)
+            cudaFree(s.buf);
+        s.buf = nullptr;
+        s.cap = 0;
+        const size_t want = (bytes + (2u << 20) - 1) & ~size_t((2u << 20) - 1);
+        cudaError_t e = cudaMalloc(&s.buf, want);
+        if (e != cudaSuccess)
+            return e;
+        s.cap = want;
+        s.used = false;
+    } else if (s.used && s.last != st) {
+        cudaError_t e = cudaStreamWaitEvent(st, s.ev, 0);
+        if (e != cudaSuccess)
+            return e;
+    }
+    *out = s.buf;
+    return cudaSuccess;
+}
+
+cudaError_t scratch_release(Scratch& s, cudaStream_t st) {
+    s.last = st;
+    s.used = true;
+    return cudaEventRecord(s.ev, st);
+}
+
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// ---- optional stage timing (measurement tools) --------------------------
+
+struct StageTiming {
+    std::mutex mu;
+    bool on = false;
+    static constexpr int kCalls = 1024;
+    cudaEvent_t ev[kCalls][4] = {};
+    int used = 0;
+    int dropped = 0;
+};
+StageTiming g_timing;
+
+// events for one call: before transform, before search, before agree, end
+cudaEvent_t* timing_slot() {
+    std::lock_guard<std::mutex> lk(g_timing.mu);
+    if (!g_timing.on)
+        return nullptr;
+    if (g_timing.used >= StageTiming::kCalls) {
+        g_timing.dropped++;
+        return nullptr;
+    }
+    cudaEvent_t* e = g_timing.ev[g_timing.used];
+    for (int i = 0; i < 4; ++i)
+        if (!e[i] && cudaEventCreate(&e[i]) != cudaSuccess)
+            return nullptr;
+    g_timing.used++;
+    return e;
+}
+
+// ---- validation ----------------------------------------------------------
+
+int elem_bytes_of(int type) {
+    switch (type) {
+        case BICOS_8U: return 1;
+        case BICOS_16U: return 2;
+        case BICOS_16S: return 2;
+        case BICOS_32F: return 4;
+        case BICOS_64F: return 8;
+        default: return 0;
+    }
+}
+
+int required_bits(int n, bool full) { return full ? n * n - 2 * n + 3 : 4 * n - 7; }
+
+int words_for(int n, bool full, int max_bits) {
+    const int bits = required_bits(n, full);
+    if (bits <= 32) return 1;
+    if (bits <= 64) return 2;
+    if (bits <= 128) return 4;
+    if (bits <= 256) return 8;
+    // past the reference's 256 bits: full mode only, up to 512 bits
+    if (full && max_bits > 256 && bits <= std::min(max_bits, 512))
+        return ((bits + 127) / 128) * 4;
+    return -1;
+}
+
+bool image_ok(const bicos_image* im, int rows, int cols, int type) {
+    return im && im->data && im->rows == rows && im->cols == cols && im->type == type &&
+           im->step >= (size_t)cols * elem_bytes_of(type);
+}
+
+bicos_status check_stacks(const bicos_image* s0, const bicos_image* s1, uint32_t n, int* eb) {
+    if (n < 2)
+        return fail(BICOS_ERR_EXCEPTION, "need at least two images");
+    if (!s0 || !s1)
+        return fail(BICOS_ERR_EXCEPTION, "null stack");
+    const int type = s0[0].type;
+    if (type != BICOS_8U && type != BICOS_16U)
+        return fail(BICOS_ERR_EXCEPTION, "bad input depths, only CV_8UC1 and CV_16UC1 are supported");
+    const int rows = s0[0].rows, cols = s0[0].cols;
+    if (rows < 1 || cols < 1)
+        return fail(BICOS_ERR_EXCEPTION, "empty images");
+    if (cols > 32767)
+        return fail(BICOS_ERR_EXCEPTION, "image width exceeds the int16 disparity range");
+    for (uint32_t i = 0; i < n; ++i)
+        if (!image_ok(&s0[i], rows, cols, type) || !image_ok(&s1[i], rows, cols, type))
+            return fail(BICOS_ERR_EXCEPTION, "all images of both stacks must share size and type");
+    *eb = elem_bytes_of(type);
+    return BICOS_OK;
+}
+
+void fill_stack(StackParams& p, const bicos_image* s0, const bicos_image* s1, uint32_t n, int eb) {
+    std::memset(&p, 0, sizeof p);
+    for (uint32_t t = 0; t < n; ++t) {
+        p.frame[0][t] = static_cast<const uint8_t*>(s0[t].data);
+        p.pitch[0][t] = (long long)s0[t].step;
+        p.frame[1][t] = static_cast<const uint8_t*>(s1 ? s1[t].data : s0[t].data);
+        p.pitch[1][t] = (long long)(s1 ? s1[t].step : s0[t].step);
+    }
+    p.n = (int)n;
+    p.rows = s0[0].rows;
+    p.cols = s0[0].cols;
+    p.elem_bytes = eb;
+}
+
+bool step_ok(float step) { return std::isfinite(step) && step >= 1e-4f; }
+
+struct DeviceGuard {
+    int dev = 0;
+    cudaError_t err = cudaSuccess;
+    DeviceGuard() { err = cudaGetDevice(&dev); }
+};
+
+}  // namespace
+
+extern "C" {
+
+const char* bicos_version(void) { return "bicos_gb300 0.1.0 (libBICOS 2.2.0 matching path, sm_103a)"; }
+
+const char* bicos_last_error(void) { return g_last_error.c_str(); }
+
+bicos_status bicos_config_default(bicos_config* c) {
+    if (!c)
+        return fail(BICOS_ERR_INVALID_ARGUMENT, "null config");
+    std::memset(c, 0, sizeof *c);
+    c->has_threshold = 1;
+    c->nxcorr_threshold = 0.5f;
+    c->mode = BICOS_MODE_LIMITED;
+    c->precision = BICOS_PRECISION_SINGLE;
+    c->variant = BICOS_VARIANT_NODUPLICATES;
+    c->max_lr_diff = 1;
+    c->no_dupes = 0;
+    c->max_bits = 256;
+    return BICOS_OK;
+}
+
+bicos_status bicos_output_types(const bicos_config* cfg, int32_t* dt, int32_t* ct) {
+    if (!cfg || !dt || !ct)
+        return fail(BICOS_ERR_INVALID_ARGUMENT, "null argument");
+    const bool thr = cfg->has_threshold != 0;
+    *dt = (thr && cfg->has_subpixel_step) ? BICOS_32F : BICOS_16S;
+    *ct = thr ? (cfg->precision == BICOS_PRECISION_DOUBLE ? BICOS_64F : BICOS_32F) : -1;
+    return BICOS_OK;
+}
+
+int32_t bicos_descriptor_words(uint32_t n, int32_t mode, int32_t max_bits) {
+    if (n < 2 || n > (uint32_t)kMaxFrames)
+        return -1;
+    return words_for((int)n, mode == BICOS_MODE_FULL, max_bits);
+}
+
+bicos_status bicos_stage_timing(int32_t enable) {
+    std::lock_guard<std::mutex> lk(g_timing.mu);
+    g_timing.on = enable != 0;
+    g_timing.used = 0;
+    g_timing.dropped = 0;
+    return BICOS_OK;
+}
+
+bicos_status bicos_stage_times(float* ms, int32_t* calls) {
+    if (!ms || !calls)
+        return fail(BICOS_ERR_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> lk(g_timing.mu);
+    ms[0] = ms[1] = ms[2] = 0.f;
+    for (int c = 0; c < g_timing.used; ++c) {
+        cudaEvent_t* e = g_timing.ev[c];
+        BICOS_CUDA_TRY(cudaEventSynchronize(e[3]));
+        for (int i = 0; i < 3; ++i) {
+            float t = 0.f;
+            BICOS_CUDA_TRY(cudaEventElapsedTime(&t, e[i], e[i + 1]));
+            ms[i] += t;
+        }
+    }
+    *calls = g_timing.used;
+    g_timing.used = 0;
+    return BICOS_OK;
+}
+
+bicos_status bicos_release_scratch(void) {
+    DeviceGuard g;
+    if (g.err != cudaSuccess)
+        return cuda_fail(g.err, "cudaGetDevice");
+    for (Scratch* sp : {&g_scratch[g.dev % kMaxDevices], &g_staging[g.dev % kMaxDevices]}) {
+        Scratch& s = *sp;
+        std::lock_guard<std::mutex> lk(s.mu);
+        if (s.used && s.ev)
+            cudaEventSynchronize(s.ev);
+        if (s.buf)
+            BICOS_CUDA_TRY(cudaFree(s.buf));
+        s.buf = nullptr;
+        s.cap = 0;
+        s.used = false;
+    }
+    return BICOS_OK;
+}
+
+bicos_status bicos_match_v1(const bicos_image* stack0, const bicos_image* stack1, uint32_t n,
+                            bicos_image* disparity, bicos_image* corrmap, const bicos_config* cfg,
+                            bicos_stream_t stream) {
+    if (!cfg)
+        return fail(BICOS_ERR_INVALID_ARGUMENT, "null config");
+    int eb = 0;
+    if (bicos_status s = check_stacks(stack0, stack1, n, &eb))
+        return s;
+    const bool full = cfg->mode == BICOS_MODE_FULL;
+    const int bits = required_bits((int)n, full);
+    const int nw = n <= (uint32_t)kMaxFrames ? words_for((int)n, full, cfg->max_bits) : -1;
+    if (nw < 0)
+        return fail(BICOS_ERR_INVALID_ARGUMENT,
+                    "input stacks too large, would require " + std::to_string(bits) + " bits");
+    const int rows = stack0[0].rows, cols = stack0[0].cols;
+    const bool thr = cfg->has_threshold != 0;
+    const bool sub = thr && cfg->has_subpixel_step != 0;
+    const bool dbl = cfg->precision == BICOS_PRECISION_DOUBLE;
+    if (sub && !step_ok(cfg->subpixel_step))
+        return fail(BICOS_ERR_EXCEPTION, "subpixel step must be a finite value >= 1e-4");
+    const bool consistency = cfg->variant == BICOS_VARIANT_CONSISTENCY;
+    if (!image_ok(disparity, rows, cols, sub ? BICOS_32F : BICOS_16S))
+        return fail(BICOS_ERR_EXCEPTION, sub ? "disparity must be a float32 image of the stack's size"
+                                             : "disparity must be an int16 image of the stack's size");
+    if (thr && corrmap && !image_ok(corrmap, rows, cols, dbl ? BICOS_64F : BICOS_32F))
+        return fail(BICOS_ERR_EXCEPTION, dbl ? "corrmap must be a float64 image of the stack's size"
+                                             : "corrmap must be a float32 image of the stack's size");
+
+    DeviceGuard g;
+    if (g.err != cudaSuccess)
+        return cuda_fail(g.err, "cudaGetDevice");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+
+    // scratch: descriptors of both sides, raw disparity, consistency bests
+    const size_t px = (size_t)rows * cols;
+    const size_t desc_bytes = align_up(px * nw * 4, 256);
+    const size_t raw_bytes = sub ? align_up(px * 2, 256) : 0;
+    const size_t best_bytes = consistency ? align_up(px * 4, 256) : 0;
+    const size_t need = 2 * desc_bytes + raw_bytes + 2 * best_bytes;
+
+    Scratch& s = g_scratch[g.dev % kMaxDevices];
+    std::lock_guard<std::mutex> lk(s.mu);
+    void* base = nullptr;
+    BICOS_CUDA_TRY(scratch_acquire(s, need, st, &base));
+    char* b = static_cast<char*>(base);
+    uint32_t* d0 = reinterpret_cast<uint32_t*>(b);
+    uint32_t* d1 = reinterpret_cast<uint32_t*>(b + desc_bytes);
+    int16_t* raw = sub ? reinterpret_cast<int16_t*>(b + 2 * desc_bytes) : static_cast<int16_t*>(disparity->data);
+    const long long raw_pitch = sub ? (long long)cols * 2 : (long long)disparity->step;
+    int32_t* fwd = consistency ? reinterpret_cast<int32_t*>(b + 2 * desc_bytes + raw_bytes) : nullptr;
+    int32_t* rev = consistency ? reinterpret_cast<int32_t*>(b + 2 * desc_bytes + raw_bytes + best_bytes) : nullptr;
+
+    AgreeParams ap;
+    std::memset(&ap, 0, sizeof ap);
+    fill_stack(ap.s, stack0, stack1, n, eb);
+
+    cudaEvent_t* tev = timing_slot();
+    if (tev)
+        cudaEventRecord(tev[0], st);
+    cudaError_t e = launch_transform(ap.s, 2, full, nw, d0, d1, st);
+    if (tev)
+        cudaEventRecord(tev[1], st);
+    if (e == cudaSuccess) {
+        if (consistency) {
+            e = launch_search(d0, d1, rows, cols, nw, cfg->no_dupes != 0, 2, nullptr, 0, fwd, rev, st);
+            if (e == cudaSuccess)
+                e = launch_consistency(fwd, rev, rows, cols, cfg->max_lr_diff, raw, raw_pitch, st);
+        } else {
+            e = launch_search(d0, d1, rows, cols, nw, true, 1, raw, raw_pitch, nullptr, nullptr, st);
+        }
+    }
+    if (tev)
+        cudaEventRecord(tev[2], st);
+    if (e == cudaSuccess && thr) {
+        ap.thr = cfg->nxcorr_threshold;
+        ap.step = sub ? cfg->subpixel_step : -1.f;
+        ap.has_minvar = cfg->has_min_variance != 0;
+        ap.minvar = cfg->has_min_variance ? cfg->min_variance * (float)n : 0.f;  // src/impl/cpu.cpp:123
+        ap.corr = corrmap ? corrmap->data : nullptr;
+        ap.corr_pitch = corrmap ? (long long)corrmap->step : 0;
+        if (sub) {
+            ap.raw = raw;
+            ap.raw_pitch = raw_pitch;
+            ap.out = disparity->data;
+            ap.out_pitch = (long long)disparity->step;
+            e = launch_agree_subpixel(ap, dbl, st);
+        } else {
+            ap.raw_io = raw;
+            ap.raw_pitch = raw_pitch;
+            e = launch_agree(ap, dbl, st);
+        }
+    }
+    if (tev)
+        cudaEventRecord(tev[3], st);
+    cudaError_t er = scratch_release(s, st);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "bicos_match_v1 launch");
+    if (er != cudaSuccess)
+        return cuda_fail(er, "cudaEventRecord");
+    return BICOS_OK;
+}
+
+bicos_status bicos_match_host_v1(const void* const* frames0, const void* const* frames1, uint32_t n, int32_t rows,
+                                 int32_t cols, int32_t type, size_t host_step, void* disparity,
+                                 size_t disparity_step, void* corrmap, size_t corrmap_step, const bicos_config* cfg,
+                                 bicos_stream_t stream) {
+    if (!cfg || !frames0 || !frames1 || !disparity)
+        return fail(BICOS_ERR_INVALID_ARGUMENT, "null argument");
+    if (n < 2)
+        return fail(BICOS_ERR_EXCEPTION, "need at least two images");
+    if (type != BICOS_8U && type != BICOS_16U)
+        return fail(BICOS_ERR_EXCEPTION, "bad input depths, only CV_8UC1 and CV_16UC1 are supported");
+    if (rows < 1 || cols < 1)
+        return fail(BICOS_ERR_EXCEPTION, "empty images");
+    const int eb = elem_bytes_of(type);
+    if (host_step < (size_t)cols * eb)
+        return fail(BICOS_ERR_INVALID_ARGUMENT, "host row step smaller than a row");
+    const bool full = cfg->mode == BICOS_MODE_FULL;
+    if (n > (uint32_t)kMaxFrames || words_for((int)n, full, cfg->max_bits) < 0)
+        return fail(BICOS_ERR_INVALID_ARGUMENT, "input stacks too large, would require " +
+                                                    std::to_string(required_bits((int)n, full)) + " bits");
+    int32_t dt = 0, ct = 0;
+    bicos_output_types(cfg, &dt, &ct);
+    const bool want_corr = corrmap && ct >= 0;
+
+    DeviceGuard g;
+    if (g.err != cudaSuccess)
+        return cuda_fail(g.err, "cudaGetDevice");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const size_t plane = align_up((size_t)rows * cols * eb, 256);
+    const size_t disp_bytes = align_up((size_t)rows * cols * elem_bytes_of(dt), 256);
+    const size_t corr_bytes = want_corr ? align_up((size_t)rows * cols * elem_bytes_of(ct), 256) : 0;
+    Scratch& s = g_staging[g.dev % kMaxDevices];
+    std::lock_guard<std::mutex> lk(s.mu);
+    void* base = nullptr;
+    BICOS_CUDA_TRY(scratch_acquire(s, 2 * n * plane + disp_bytes + corr_bytes, st, &base));
+    char* b = static_cast<char*>(base);
+    bicos_image im0[kMaxFrames], im1[kMaxFrames];
+    for (uint32_t t = 0; t < n; ++t) {
+        char* p0 = b + (size_t)t * plane;
+        char* p1 = b + (size_t)(n + t) * plane;
+        BICOS_CUDA_TRY(cudaMemcpy2DAsync(p0, (size_t)cols * eb, frames0[t], host_step, (size_t)cols * eb, rows,
+                                         cudaMemcpyHostToDevice, st));
+        BICOS_CUDA_TRY(cudaMemcpy2DAsync(p1, (size_t)cols * eb, frames1[t], host_step, (size_t)cols * eb, rows,
+                                         cudaMemcpyHostToDevice, st));
+        im0[t] = bicos_image {p0, (size_t)cols * eb, rows, cols, type, 0};
+        im1[t] = bicos_image {p1, (size_t)cols * eb, rows, cols, type, 0};
+    }
+    char* dd = b + 2 * (size_t)n * plane;
+    char* cd = dd + disp_bytes;
+    bicos_image dimg {dd, (size_t)cols * elem_bytes_of(dt), rows, cols, dt, 0};
+    bicos_image cimg {cd, want_corr ? (size_t)cols * elem_bytes_of(ct) : 0, rows, cols, ct, 0};
+    bicos_status rs = bicos_match_v1(im0, im1, n, &dimg, want_corr ? &cimg : nullptr, cfg, stream);
+    if (rs == BICOS_OK) {
+        cudaError_t e = cudaMemcpy2DAsync(disparity, disparity_step, dd, dimg.step, dimg.step, rows,
+                                          cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess && want_corr)
+            e = cudaMemcpy2DAsync(corrmap, corrmap_step, cd, cimg.step, cimg.step, rows, cudaMemcpyDeviceToHost, st);
+        if (e != cudaSuccess)
+            rs = cuda_fail(e, "cudaMemcpy2DAsync (download)");
+    }
+    cudaError_t er = scratch_release(s, st);
+    cudaError_t es = cudaStreamSynchronize(st);
+    if (rs != BICOS_OK)
+        return rs;
+    if (er != cudaSuccess)
+        return cuda_fail(er, "cudaEventRecord");
+    if (es != cudaSuccess)
+        return cuda_fail(es, "cudaStreamSynchronize");
+    return BICOS_OK;
+}
+
+bicos_status bicos_descriptor_transform_v1(const bicos_image* stack, uint32_t n, int32_t mode, uint32_t nwords,
+                                           uint32_t* descriptors, bicos_stream_t stream) {
+    int eb = 0;
+    if (bicos_status s = check_stacks(stack, stack, n, &eb))
+        return s;
+    const bool full = mode == BICOS_MODE_FULL;
+    const int nw = n <= (uint32_t)kMaxFrames ? words_for((int)n, full, 512) : -1;
+    if (nw < 0)
+        return fail(BICOS_ERR_INVALID_ARGUMENT, "input stacks too large, would require " +
+                                                    std::to_string(required_bits((int)n, full)) + " bits");
+    if ((int)nwords != nw)
+        return fail(BICOS_ERR_INVALID_ARGUMENT, "descriptor width does not match the stack size and mode");
+    if (!descriptors)
+        return fail(BICOS_ERR_INVALID_ARGUMENT, "null descriptor buffer");
+    StackParams p;
+    fill_stack(p, stack, nullptr, n, eb);
+    cudaError_t e = launch_transform(p, 1, full, nw, descriptors, descriptors, reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess)
+        return cuda_fail(e, "descriptor transform launch");
+    return BICOS_OK;
+}
+
+bicos_status bicos_search_v1(const uint32_t* desc0, const uint32_t* desc1, int32_t rows, int32_t cols,
+                             uint32_t nwords, int32_t flags, int32_t max_lr_diff, bicos_image* disparity,
+                             bicos_stream_t stream) {
+    if (!desc0 || !desc1 || rows < 1 || cols < 1 || cols > 32767)
+        return fail(BICOS_ERR_INVALID_ARGUMENT, "bad descriptor arguments");
+    if (nwords != 1 && nwords != 2 && nwords != 4 && nwords != 8 && nwords != 12 && nwords != 16)
+        return fail(BICOS_ERR_INVALID_ARGUMENT, "unsupported descriptor width");
+    if (!image_ok(disparity, rows, cols, BICOS_16S))
+        return fail(BICOS_ERR_EXCEPTION, "disparity must be an int16 image of the descriptor size");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const bool nodup = (flags & BICOS_FLAG_NODUPES) != 0;
+    cudaError_t e;
+    if (flags & BICOS_FLAG_CONSISTENCY) {
+        DeviceGuard g;
+        if (g.err != cudaSuccess)
+            return cuda_fail(g.err, "cudaGetDevice");
+        Scratch& s = g_scratch[g.dev % kMaxDevices];
+        std::lock_guard<std::mutex> lk(s.mu);
+        const size_t bb = align_up((size_t)rows * cols * 4, 256);
+        void* base = nullptr;
+        BICOS_CUDA_TRY(scratch_acquire(s, 2 * bb, st, &base));
+        int32_t* fwd = static_cast<int32_t*>(base);
+        int32_t* rev = reinterpret_cast<int32_t*>(static_cast<char*>(base) + bb);
+        e = launch_search(desc0, desc1, rows, cols, (int)nwords, nodup, 2, nullptr, 0, fwd, rev, st);
+        if (e == cudaSuccess)
+            e = launch_consistency(fwd, rev, rows, cols, max_lr_diff, static_cast<int16_t*>(disparity->data),
+                                   (long long)disparity->step, st);
+        cudaError_t er = scratch_release(s, st);
+        if (e == cudaSuccess)
+            e = er;
+    } else {
+        e = launch_search(desc0, desc1, rows, cols, (int)nwords, nodup, 1, static_cast<int16_t*>(disparity->data),
+                          (long long)disparity->step, nullptr, nullptr, st);
+    }
+    if (e != cudaSuccess)
+        return cuda_fail(e, "search launch");
+    return BICOS_OK;
+}
+
+bicos_status bicos_agree_v1(bicos_image* disparity, const bicos_image* stack0, const bicos_image* stack1,
+                            uint32_t n, float nxcorr_threshold, int32_t has_min_var, float min_var,
+                            int32_t precision, bicos_image* corrmap, bicos_stream_t stream) {
+    int eb = 0;
+    if (bicos_status s = check_stacks(stack0, stack1, n, &eb))
+        return s;
+    if (n > (uint32_t)kMaxFrames)
+        return fail(BICOS_ERR_EXCEPTION, "Bad number of images");
+    const int rows = stack0[0].rows, cols = stack0[0].cols;
+    const bool dbl = precision == BICOS_PRECISION_DOUBLE;
+    if (!image_ok(disparity, rows, cols, BICOS_16S))
+        return fail(BICOS_ERR_EXCEPTION, "disparity must be an int16 image of the stack's size");
+    if (corrmap && !image_ok(corrmap, rows, cols, dbl ? BICOS_64F : BICOS_32F))
+        return fail(BICOS_ERR_EXCEPTION, "corrmap type or size mismatch");
+    AgreeParams ap;
+    std::memset(&ap, 0, sizeof ap);
+    fill_stack(ap.s, stack0, stack1, n, eb);
+    ap.raw_io = static_cast<int16_t*>(disparity->data);
+    ap.raw_pitch = (long long)disparity->step;
+    ap.thr = nxcorr_threshold;
+    ap.has_minvar = has_min_var != 0;
+    ap.minvar = min_var;
+    ap.corr = corrmap ? corrmap->data : nullptr;
+    ap.corr_pitch = corrmap ? (long long)corrmap->step : 0;
+    cudaError_t e = launch_agree(ap, dbl, reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess)
+        return cuda_fail(e, "agree launch");
+    return BICOS_OK;
+}
+
+bicos_status bicos_agree_subpixel_v1(const bicos_image* raw_disparity, const bicos_image* stack0,
+                                     const bicos_image* stack1, uint32_t n, float nxcorr_threshold,
+                                     float subpixel_step, int32_t has_min_var, float min_var, int32_t precision,
+                                     bicos_image* disparity, bicos_image* corrmap, bicos_stream_t stream) {
+    int eb = 0;
+    if (bicos_status s = check_stacks(stack0, stack1, n, &eb))
+        return s;
+    if (n > (uint32_t)kMaxFrames)
+        return fail(BICOS_ERR_EXCEPTION, "Bad number of images");
+    const int rows = stack0[0].rows, cols = stack0[0].cols;
+    const bool dbl = precision == BICOS_PRECISION_DOUBLE;
+    if (!step_ok(subpixel_step))
+        return fail(BICOS_ERR_EXCEPTION, "subpixel step must be a finite value >= 1e-4");
+    if (!image_ok(raw_disparity, rows, cols, BICOS_16S))
+        return fail(BICOS_ERR_EXCEPTION, "raw disparity must be an int16 image of the stack's size");
+    if (!image_ok(disparity, rows, cols, BICOS_32F))
+        return fail(BICOS_ERR_EXCEPTION, "disparity must be a float32 image of the stack's size");
+    if (corrmap && !image_ok(corrmap, rows, cols, dbl ? BICOS_64F : BICOS_32F))
+        return fail(BICOS_ERR_EXCEPTION, "corrmap type or size mismatch");
+    AgreeParams ap;
+    std::memset(&ap, 0, sizeof ap);
+    fill_stack(ap.s, stack0, stack1, n, eb);
+    ap.raw = static_cast<const int16_t*>(raw_disparity->data);
+    ap.raw_pitch = (long long)raw_disparity->step;
+    ap.out = disparity->data;
+    ap.out_pitch = (long long)disparity->step;
+    ap.thr = nxcorr_threshold;
+    ap.step = subpixel_step;
+    ap.has_minvar = has_min_var != 0;
+    ap.minvar = min_var;
+    ap.corr = corrmap ? corrmap->data : nullptr;
+    ap.corr_pitch = corrmap ? (long long)corrmap->step : 0;
+    cudaError_t e = launch_agree_subpixel(ap, dbl, reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess)
+        return cuda_fail(e, "agree_subpixel launch");
+    return BICOS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,58 @@
+// Internal interface between the host orchestration (capi.cu) and the
+// sm_103a kernels (transform.cu, search.cu, agree.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace bicos_gb300 {
+
+constexpr int kMaxFrames = 65;      // limited mode, 256-bit descriptors (4*65-7 = 253)
+constexpr int kMaxFullFrames = 23;  // full mode, 512-bit extension (23^2-2*23+3 = 486)
+constexpr int16_t kInvalidDisp = INT16_MIN;
+
+// Frame pointers and row pitches of both sides, passed by value
+// (__grid_constant__) so kernels read them from the constant bank.
+struct StackParams {
+    const uint8_t* frame[2][kMaxFrames];
+    long long pitch[2][kMaxFrames];
+    int n;
+    int rows;
+    int cols;
+    int elem_bytes;
+};
+
+struct AgreeParams {
+    StackParams s;
+    const int16_t* raw;   // int16 disparity in (subpixel) / in-out (agree)
+    long long raw_pitch;
+    int16_t* raw_io;
+    void* out;            // float disparity (subpixel)
+    long long out_pitch;
+    void* corr;           // float or double corrmap, may be null
+    long long corr_pitch;
+    float thr;
+    float step;
+    int has_minvar;
+    float minvar;
+};
+
+cudaError_t launch_transform(const StackParams& p, int sides, bool full, int nwords,
+                             uint32_t* desc0, uint32_t* desc1, cudaStream_t st);
+
+// Row-wise arg-min.  When disp != nullptr (one direction, NODUPES or plain)
+// the kernel writes int16 disparities col0 - best directly; otherwise it
+// writes int32 best columns (-1 = invalid) of each direction to best0/best1.
+cudaError_t launch_search(const uint32_t* desc0, const uint32_t* desc1, int rows, int cols,
+                          int nwords, bool nodupes, int directions, int16_t* disp,
+                          long long disp_pitch, int32_t* best0, int32_t* best1,
+                          cudaStream_t st);
+
+cudaError_t launch_consistency(const int32_t* fwd, const int32_t* rev, int rows, int cols,
+                               int max_lr_diff, int16_t* disp, long long disp_pitch,
+                               cudaStream_t st);
+
+cudaError_t launch_agree(const AgreeParams& p, bool dbl, cudaStream_t st);
+cudaError_t launch_agree_subpixel(const AgreeParams& p, bool dbl, cudaStream_t st);
+
+}  // namespace bicos_gb300

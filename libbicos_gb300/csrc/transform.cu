@@ -1,0 +1,217 @@
+// Binary temporal descriptor transform (stage a).
+//
+// Semantics follow libBICOS include/impl/cpu/descriptor_transform.hpp:31-123
+// (and the CUDA kernels include/impl/cuda/descriptor_transform.cuh:30-149):
+// bit i of the descriptor is set LSB-first, word i/32.  Design: one thread
+// per pixel, both sides in one launch (blockIdx.z), the n samples held in
+// registers, every bit position a compile-time constant (loops fully
+// unrolled over the bucket maximum), so the descriptor words never leave
+// registers.  The temporal mean is the reference's float RN(sum / n); the
+// sum is exact in int, and `a < mean` is evaluated as `a < ceil(mean)`,
+// which is the same predicate for integer a.
+#include "kernels.cuh"
+
+namespace bicos_gb300 {
+namespace {
+
+template<int NW>
+__device__ __forceinline__ void set_bit(uint32_t (&w)[NW], int pos, bool v) {
+    w[pos >> 5] |= (uint32_t)v << (pos & 31);
+}
+
+// position known only at run time: select the word without local memory
+template<int NW>
+__device__ __forceinline__ void set_bit_dyn(uint32_t (&w)[NW], int pos, bool v) {
+    const uint32_t m = (uint32_t)v << (pos & 31);
+    const int k = pos >> 5;
+#pragma unroll
+    for (int j = 0; j < NW; ++j)
+        if (j == k)
+            w[j] |= m;
+}
+
+template<typename T>
+__device__ __forceinline__ int ld_px(const StackParams& p, int side, int t, int row, int col) {
+    const T* r = reinterpret_cast<const T*>(p.frame[side][t] + (long long)row * p.pitch[side][t]);
+    return (int)__ldg(r + col);
+}
+
+template<int NW>
+__device__ __forceinline__ void store_desc(uint32_t* out, const uint32_t (&w)[NW]) {
+    if constexpr (NW % 4 == 0) {
+        uint4* o = reinterpret_cast<uint4*>(out);
+#pragma unroll
+        for (int j = 0; j < NW / 4; ++j)
+            o[j] = make_uint4(w[4 * j], w[4 * j + 1], w[4 * j + 2], w[4 * j + 3]);
+    } else if constexpr (NW == 2) {
+        *reinterpret_cast<uint2*>(out) = make_uint2(w[0], w[1]);
+    } else {
+        out[0] = w[0];
+    }
+}
+
+__host__ __device__ constexpr int words_for_bits(int bits) {
+    return bits <= 32 ? 1 : bits <= 64 ? 2 : bits <= 128 ? 4 : bits <= 256 ? 8 : ((bits + 127) / 128) * 4;
+}
+
+// limited mode: 3 bits per t < n-2 plus a pair-sum bit from t >= 2, 4 tail bits
+template<typename T, int NW, int NMAX>
+__global__ void __launch_bounds__(256) k_transform_limited(const __grid_constant__ StackParams p,
+                                                           uint32_t* __restrict__ d0,
+                                                           uint32_t* __restrict__ d1) {
+    const int col = blockIdx.x * blockDim.x + threadIdx.x;
+    const int row = blockIdx.y, side = blockIdx.z;
+    if (col >= p.cols)
+        return;
+    const int n = p.n;
+
+    int v[NMAX];
+    int sum = 0;
+#pragma unroll
+    for (int t = 0; t < NMAX; ++t) {
+        v[t] = t < n ? ld_px<T>(p, side, t, row, col) : 0;
+        sum += v[t];
+    }
+    const float av = __fdiv_rn((float)sum, (float)n);
+    const int iav = (int)ceilf(av);  // a < av  <=>  a < ceil(av) for integer a
+
+    uint32_t w[NW];
+#pragma unroll
+    for (int j = 0; j < NW; ++j)
+        w[j] = 0u;
+
+    int a = v[0], b = v[1];
+    int pp = -1, p1 = -1;  // pair sums of steps t-2 and t-1 (reference's prev_pair_sums ring)
+#pragma unroll
+    for (int t = 0; t < NMAX - 2; ++t) {
+        if (t < n - 2) {
+            const int c = v[t + 2];
+            const int pos = 3 * t + (t >= 2 ? t - 2 : 0);
+            set_bit(w, pos, a < b);
+            set_bit(w, pos + 1, a < c);
+            set_bit(w, pos + 2, a < iav);
+            const int cur = a + b;
+            if (t >= 2)
+                set_bit(w, pos + 3, pp < cur);
+            pp = p1;
+            p1 = cur;
+            a = b;
+            b = c;
+        }
+    }
+    const int pos = 3 * (n - 2) + max(0, n - 4);
+    set_bit_dyn(w, pos, a < b);
+    set_bit_dyn(w, pos + 1, a < iav);
+    set_bit_dyn(w, pos + 2, b < iav);
+    set_bit_dyn(w, pos + 3, pp < a + b);
+
+    store_desc(((side ? d1 : d0) + ((size_t)row * p.cols + col) * NW), w);
+}
+
+// full mode: 3 bits per t < n-2, 3 tail bits, then every ordered pair of
+// non-adjacent pair sums; n is a template parameter so every position is
+// a constant
+template<typename T, int N>
+__global__ void __launch_bounds__(256) k_transform_full(const __grid_constant__ StackParams p,
+                                                        uint32_t* __restrict__ d0,
+                                                        uint32_t* __restrict__ d1) {
+    constexpr int NW = words_for_bits(N * N - 2 * N + 3);
+    const int col = blockIdx.x * blockDim.x + threadIdx.x;
+    const int row = blockIdx.y, side = blockIdx.z;
+    if (col >= p.cols)
+        return;
+
+    int v[N];
+    int sum = 0;
+#pragma unroll
+    for (int t = 0; t < N; ++t) {
+        v[t] = ld_px<T>(p, side, t, row, col);
+        sum += v[t];
+    }
+    const float av = __fdiv_rn((float)sum, (float)N);
+    const int iav = (int)ceilf(av);
+
+    uint32_t w[NW];
+#pragma unroll
+    for (int j = 0; j < NW; ++j)
+        w[j] = 0u;
+
+    int ps[N - 1];
+    int pos = 0;
+#pragma unroll
+    for (int t = 0; t < N - 2; ++t) {
+        set_bit(w, pos++, v[t] < v[t + 1]);
+        set_bit(w, pos++, v[t] < v[t + 2]);
+        set_bit(w, pos++, v[t] < iav);
+    }
+#pragma unroll
+    for (int t = 0; t < N - 1; ++t)
+        ps[t] = v[t] + v[t + 1];
+    set_bit(w, pos++, v[N - 2] < v[N - 1]);
+    set_bit(w, pos++, v[N - 2] < iav);
+    set_bit(w, pos++, v[N - 1] < iav);
+#pragma unroll
+    for (int t = 0; t < N - 1; ++t)
+#pragma unroll
+        for (int i = 0; i < N - 1; ++i) {
+            if (i == t || i == t - 1 || i == t + 1)
+                continue;
+            set_bit(w, pos++, ps[t] < ps[i]);
+        }
+
+    store_desc(((side ? d1 : d0) + ((size_t)row * p.cols + col) * NW), w);
+}
+
+template<typename T>
+using tf_kernel_t = void (*)(StackParams, uint32_t*, uint32_t*);
+
+template<typename T>
+tf_kernel_t<T> pick_full(int n) {
+    switch (n) {
+#define BICOS_FULL_CASE(N) \
+    case N: return k_transform_full<T, N>;
+        BICOS_FULL_CASE(2) BICOS_FULL_CASE(3) BICOS_FULL_CASE(4) BICOS_FULL_CASE(5)
+        BICOS_FULL_CASE(6) BICOS_FULL_CASE(7) BICOS_FULL_CASE(8) BICOS_FULL_CASE(9)
+        BICOS_FULL_CASE(10) BICOS_FULL_CASE(11) BICOS_FULL_CASE(12) BICOS_FULL_CASE(13)
+        BICOS_FULL_CASE(14) BICOS_FULL_CASE(15) BICOS_FULL_CASE(16) BICOS_FULL_CASE(17)
+        BICOS_FULL_CASE(18) BICOS_FULL_CASE(19) BICOS_FULL_CASE(20) BICOS_FULL_CASE(21)
+        BICOS_FULL_CASE(22) BICOS_FULL_CASE(23)
+#undef BICOS_FULL_CASE
+        default: return nullptr;
+    }
+}
+
+template<typename T>
+tf_kernel_t<T> pick_limited(int nwords) {
+    switch (nwords) {
+        case 1: return k_transform_limited<T, 1, 9>;
+        case 2: return k_transform_limited<T, 2, 17>;
+        case 4: return k_transform_limited<T, 4, 33>;
+        case 8: return k_transform_limited<T, 8, 65>;
+        default: return nullptr;
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_transform(const StackParams& p, int sides, bool full, int nwords, uint32_t* desc0,
+                             uint32_t* desc1, cudaStream_t st) {
+    void (*k)(StackParams, uint32_t*, uint32_t*) = nullptr;
+    if (full) {
+        if (words_for_bits(p.n * p.n - 2 * p.n + 3) != nwords)
+            return cudaErrorInvalidValue;
+        k = p.elem_bytes == 1 ? pick_full<uint8_t>(p.n) : pick_full<uint16_t>(p.n);
+    } else {
+        if (words_for_bits(4 * p.n - 7) != nwords)
+            return cudaErrorInvalidValue;
+        k = p.elem_bytes == 1 ? pick_limited<uint8_t>(nwords) : pick_limited<uint16_t>(nwords);
+    }
+    if (!k)
+        return cudaErrorInvalidValue;
+    const dim3 block(256);
+    const dim3 grid((p.cols + 255) / 256, p.rows, sides);
+    k<<<grid, block, 0, st>>>(p, desc0, desc1);
+    return cudaGetLastError();
+}
+
+}  // namespace bicos_gb300

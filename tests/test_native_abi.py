@@ -1,0 +1,112 @@
+"""The C-ABI library builds, loads and exports every entry point that
+include/bicos_c.h declares; host-side validation and error behaviour work
+without a GPU (no compute is launched here)."""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+
+def declared_symbols():
+    src = open(os.path.join(ROOT, "include", "bicos_c.h")).read()
+    decl = r"^(?:const\s+)?[A-Za-z_]\w*\s*\*?\s*(bicos_\w+)\s*\("
+    return sorted(set(re.findall(decl, src, re.MULTILINE)))
+
+
+def test_exports_every_declared_symbol(native):
+    so = native.lib_path()
+    out = subprocess.run(["nm", "-D", "--defined-only", so], capture_output=True, text=True, check=True).stdout
+    exported = set(re.findall(r" T (\w+)", out))
+    missing = [s for s in declared_symbols() if s not in exported]
+    assert not missing, missing
+    lib = native.load()
+    for s in declared_symbols():
+        assert hasattr(lib, s)
+
+
+def test_cpp_api_exported(native):
+    out = subprocess.run(["nm", "-DC", "--defined-only", native.lib_path()], capture_output=True, text=True,
+                         check=True).stdout
+    assert "BICOS::match(" in out
+    assert "BICOS::Image::create(" in out
+
+
+def test_config_defaults(native):
+    c = native.default_config()  # include/common.hpp:73-82
+    assert c.has_threshold == 1 and abs(c.nxcorr_threshold - 0.5) < 1e-7
+    assert c.has_subpixel_step == 0 and c.has_min_variance == 0
+    assert c.mode == 0 and c.precision == 0 and c.variant == 0
+    assert c.max_lr_diff == 1 and c.no_dupes == 0 and c.max_bits == 256
+
+
+def test_output_types(native):
+    lib = native.load()
+    c = native.default_config()
+    dt, ct = C.c_int32(), C.c_int32()
+    lib.bicos_output_types(C.byref(c), C.byref(dt), C.byref(ct))
+    assert (dt.value, ct.value) == (native.BICOS_16S, native.BICOS_32F)
+    c.has_subpixel_step, c.subpixel_step, c.precision = 1, 0.1, 1
+    lib.bicos_output_types(C.byref(c), C.byref(dt), C.byref(ct))
+    assert (dt.value, ct.value) == (native.BICOS_32F, native.BICOS_64F)
+    c.has_threshold = 0
+    lib.bicos_output_types(C.byref(c), C.byref(dt), C.byref(ct))
+    assert (dt.value, ct.value) == (native.BICOS_16S, -1)
+
+
+def test_descriptor_words_table(native, oracle):
+    lib = native.load()
+    for n in range(2, 66):
+        for mode in (0, 1):
+            for mb in (256, 512):
+                want = oracle.descriptor_words(oracle.required_bits(n, mode == 1), mb)
+                if mode == 0 and want > 8:
+                    want = -1  # the 512-bit extension is for full mode only
+                assert lib.bicos_descriptor_words(n, mode, mb) == want, (n, mode, mb)
+
+
+def _stack(native, n, type_=0, rows=4, cols=8):
+    arr = (native.Image * max(n, 1))()
+    for i in range(n):
+        arr[i] = native.image(0x1000 * (i + 1), rows, cols, type_, cols * 2)
+    return arr
+
+
+def test_errors_before_any_device_work(native):
+    lib = native.load()
+    c = native.default_config()
+    d = native.image(0x10, 4, 8, native.BICOS_16S, 16)
+    s = _stack(native, 1)
+    assert lib.bicos_match_v1(s, s, 1, C.byref(d), None, C.byref(c), None) == native.ERR_EXCEPTION
+    assert lib.bicos_last_error() == b"need at least two images"
+    s = _stack(native, 3, type_=native.BICOS_32F)
+    assert lib.bicos_match_v1(s, s, 3, C.byref(d), None, C.byref(c), None) == native.ERR_EXCEPTION
+    assert lib.bicos_last_error() == b"bad input depths, only CV_8UC1 and CV_16UC1 are supported"
+    s = _stack(native, 66)
+    assert lib.bicos_match_v1(s, s, 66, C.byref(d), None, C.byref(c), None) == native.ERR_INVALID_ARGUMENT
+    assert lib.bicos_last_error() == b"input stacks too large, would require 257 bits"
+    c.mode = 1
+    s = _stack(native, 17)
+    assert lib.bicos_match_v1(s, s, 17, C.byref(d), None, C.byref(c), None) == native.ERR_INVALID_ARGUMENT
+    assert lib.bicos_last_error() == b"input stacks too large, would require 258 bits"
+    c.mode = 0
+    c.has_subpixel_step, c.subpixel_step = 1, 0.0
+    s = _stack(native, 4)
+    assert lib.bicos_match_v1(s, s, 4, C.byref(d), None, C.byref(c), None) == native.ERR_EXCEPTION
+    assert b"subpixel step" in lib.bicos_last_error()
+    # wrong output type: subpixel needs float32
+    c.subpixel_step = 0.1
+    assert lib.bicos_match_v1(s, s, 4, C.byref(d), None, C.byref(c), None) == native.ERR_EXCEPTION
+    assert b"float32" in lib.bicos_last_error()
+    # mismatched frame sizes
+    s2 = _stack(native, 4, rows=5)
+    c.has_subpixel_step = 0
+    assert lib.bicos_match_v1(s, s2, 4, C.byref(d), None, C.byref(c), None) == native.ERR_EXCEPTION
+
+
+def test_version(native):
+    assert b"sm_103a" in native.load().bicos_version()
