@@ -159,6 +159,27 @@ bicos_status bicos_search_v1(const uint32_t* desc0, const uint32_t* desc1, int32
                              int32_t cols, uint32_t nwords, int32_t flags, int32_t max_lr_diff,
                              bicos_image* disparity, bicos_stream_t stream);
 
+/*
+ * bicos_search_v1 without any device allocation.  No counterpart in the
+ * reference: for callers that cannot call cudaMalloc while they run (a
+ * real-time loop with a fixed memory plan, a host framework that owns all
+ * device memory and forbids allocation in its callbacks, code that must not
+ * meet an allocation failure or an allocator synchronisation mid-pipeline).
+ * The consistency flags need scratch for the forward and backward best
+ * columns; here it is a fixed 32 MiB device array inside the library
+ * (limit rows * cols <= 4194304 pixels, larger sizes fail with
+ * BICOS_ERR_INVALID_ARGUMENT), held by every GPU that loads it until the
+ * process exits.  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress) with that device current; make that first
+ * call before any stream capture.  All calls share the array: calls that
+ * overlap on the GPU race, so serialise them.  Without the consistency flag
+ * no scratch is used.  Outputs equal bicos_search_v1's.
+ */
+bicos_status bicos_search_noalloc_v1(const uint32_t* desc0, const uint32_t* desc1, int32_t rows,
+                                     int32_t cols, uint32_t nwords, int32_t flags,
+                                     int32_t max_lr_diff, bicos_image* disparity,
+                                     bicos_stream_t stream);
+
 /* NCC agreement in place on an int16 disparity; min_var is the per-stack
  * threshold (min_variance * n) used when has_min_var is set. */
 bicos_status bicos_agree_v1(bicos_image* disparity, const bicos_image* stack0,

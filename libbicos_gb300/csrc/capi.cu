@@ -199,6 +199,8 @@ struct DeviceGuard {
 
 }  // namespace
 
+void bicos_gb300::set_last_error(const std::string& msg) { g_last_error = msg; }
+
 extern "C" {
 
 const char* bicos_version(void) { return "bicos_gb300 0.1.0 (libBICOS 2.2.0 matching path, sm_103a)"; }

@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
+
 namespace bicos_gb300 {
 
 constexpr int kMaxFrames = 65;      // limited mode, 256-bit descriptors (4*65-7 = 253)
@@ -54,5 +56,8 @@ cudaError_t launch_consistency(const int32_t* fwd, const int32_t* rev, int rows,
 
 cudaError_t launch_agree(const AgreeParams& p, bool dbl, cudaStream_t st);
 cudaError_t launch_agree_subpixel(const AgreeParams& p, bool dbl, cudaStream_t st);
+
+// sets the per-thread message bicos_last_error() returns (defined in capi.cu)
+void set_last_error(const std::string& msg);
 
 }  // namespace bicos_gb300
