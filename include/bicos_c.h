@@ -207,6 +207,11 @@ bicos_status bicos_agree_subpixel_v1(const bicos_image* raw_disparity, const bic
 bicos_status bicos_stage_timing(int32_t enable);
 bicos_status bicos_stage_times(float* ms_per_stage /* [3] */, int32_t* calls);
 
+/* Number of kernel blocks on this device whose bounded waits ran out since
+ * load (0 in normal operation; such a block records the event instead of
+ * hanging and leaves its outputs unwritten).  Synchronises the device. */
+int32_t bicos_kernel_faults(void);
+
 /* Library version string. */
 const char* bicos_version(void);
 

@@ -70,6 +70,7 @@ def load():
         "bicos_match_host_v1": ([C.POINTER(P), C.POINTER(P), U, I, I, I, S, P, S, P, S, CFG, P], C.c_int),
         "bicos_release_scratch": ([], C.c_int),
         "bicos_stage_timing": ([I], C.c_int),
+        "bicos_kernel_faults": ([], I),
         "bicos_stage_times": ([C.POINTER(C.c_float), C.POINTER(I)], C.c_int),
         "bicos_descriptor_transform_v1": ([IMG, U, I, U, P, P], C.c_int),
         "bicos_search_v1": ([P, P, I, I, U, I, I, IMG, P], C.c_int),

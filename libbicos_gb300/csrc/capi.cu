@@ -237,6 +237,8 @@ int32_t bicos_descriptor_words(uint32_t n, int32_t mode, int32_t max_bits) {
     return words_for((int)n, mode == BICOS_MODE_FULL, max_bits);
 }
 
+int32_t bicos_kernel_faults(void) { return (int32_t)read_tc_faults(); }
+
 bicos_status bicos_stage_timing(int32_t enable) {
     std::lock_guard<std::mutex> lk(g_timing.mu);
     g_timing.on = enable != 0;

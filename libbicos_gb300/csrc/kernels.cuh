@@ -50,6 +50,15 @@ cudaError_t launch_search(const uint32_t* desc0, const uint32_t* desc1, int rows
                           long long disp_pitch, int32_t* best0, int32_t* best1,
                           cudaStream_t st);
 
+// tensor-core search (search_tc.cu): same contract as launch_search, for
+// rows of at most 4096 columns
+bool search_tc_supported(int cols);
+cudaError_t launch_search_tc(const uint32_t* desc0, const uint32_t* desc1, int rows, int cols, int nwords,
+                             bool nodupes, int directions, int16_t* disp, long long disp_pitch,
+                             int32_t* best0, int32_t* best1, cudaStream_t st);
+// number of tensor-core search CTAs whose bounded waits ran out (synchronous)
+unsigned int read_tc_faults();
+
 cudaError_t launch_consistency(const int32_t* fwd, const int32_t* rev, int rows, int cols,
                                int max_lr_diff, int16_t* disp, long long disp_pitch,
                                cudaStream_t st);

@@ -1,0 +1,406 @@
+// Row-wise Hamming arg-min on the 5th-generation tensor cores (stage b).
+//
+// Hamming distance as a dot product: with every descriptor bit mapped to
+// +1 (set) or -1 (clear), dot(a, b) = K - 2 * ham(a, b) for K-bit words, so
+// the minimum Hamming distance is the maximum dot product.  Per CTA:
+//   A = 128 query descriptors of one row (TMEM lanes), B = 128 candidate
+//   descriptors per tile, both expanded to FP8 e4m3 (+1 = 0x38, -1 = 0xB8)
+//   in shared memory in the canonical no-swizzle K-major layout;
+//   tcgen05.mma kind::f8f6f4 (M=128, N=128, K=32 per instruction) writes
+//   D = A * B^T to TMEM with FP32 accumulation (exact: |D| <= K <= 512);
+//   the epilogue reads D back with tcgen05.ld (thread = query pixel) and
+//   keeps the two largest keys  key = dot - col * 2^-12  (exact in FP32 for
+//   cols <= 4096), which carry the first arg-max and the tie test of
+//   libBICOS's bicos_search (include/impl/cpu/bicos.hpp:50-76).
+// Outputs and semantics are those of k_search (search.cu).  All waits are
+// bounded: a wait that runs out records a fault, and the CTA frees its TMEM
+// and exits.
+#include "kernels.cuh"
+
+namespace bicos_gb300 {
+
+__device__ unsigned int g_tc_faults = 0;
+
+namespace {
+
+constexpr int kRows = 128;          // MMA M = N = 128
+constexpr float kColScale = 1.0f / 4096.0f;
+constexpr int kMaxCols = 4096;      // key exactness bound
+constexpr long long kWaitCycles = 4LL << 30;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void tmem_alloc(uint32_t dst_smem, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(dst_smem), "r"(ncols)
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish() {
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void mbar_init(uint32_t addr, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(addr), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t addr, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(addr), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// canonical K-major, no swizzle: core matrix = 8 rows x 16 bytes (128 B
+// contiguous); LBO = distance of K-adjacent core matrices, SBO = distance
+// of 8-row groups; bits 46..47 = 1 (descriptor version)
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
+           (1ull << 46);
+}
+
+// kind::f8f6f4: D f32 (bits 4-5 = 1), A/B e4m3 (0), K-major, N>>3 at 17, M>>4 at 24
+constexpr uint32_t kIdesc = (1u << 4) | ((uint32_t)(kRows >> 3) << 17) | ((uint32_t)(kRows >> 4) << 24);
+
+__device__ __forceinline__ void mma_f8(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+                 : "memory");
+}
+
+// 32 consecutive FP32 columns of this warp's TMEM lane quarter
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int k = 0; k < 32; ++k)
+        v[k] = __uint_as_float(r[k]);
+}
+
+// 8 descriptor bits -> 8 FP8 values (+1 set, -1 clear)
+__device__ __forceinline__ uint32_t expand_nibble(uint32_t x) {
+    const uint32_t s = (x * 0x204081u) & 0x01010101u;  // bit i -> byte i
+    return 0xB8B8B8B8u - (s << 7);
+}
+
+// one descriptor (NW words) into row rr of a 128-row FP8 tile
+template<int NW>
+__device__ __forceinline__ void expand_row(uint8_t* tile, int rr, const uint32_t* desc, const uint2* lut) {
+    constexpr int KB = NW * 32;
+    uint4 w4[(NW + 3) / 4];
+    if constexpr (NW % 4 == 0) {
+#pragma unroll
+        for (int j = 0; j < NW / 4; ++j)
+            w4[j] = __ldg(reinterpret_cast<const uint4*>(desc) + j);
+    }
+    uint8_t* base = tile + (rr >> 3) * (8 * KB) + (rr & 7) * 16;
+#pragma unroll
+    for (int w = 0; w < NW; ++w) {
+        uint32_t x;
+        if constexpr (NW % 4 == 0) {
+            const uint4 q = w4[w >> 2];
+            x = (w & 3) == 0 ? q.x : (w & 3) == 1 ? q.y : (w & 3) == 2 ? q.z : q.w;
+        } else {
+            x = __ldg(desc + w);
+        }
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const uint2 l0 = lut[(x >> (16 * h)) & 0xFFu];
+            const uint2 l1 = lut[(x >> (16 * h + 8)) & 0xFFu];
+            *reinterpret_cast<uint4*>(base + (2 * w + h) * 128) = make_uint4(l0.x, l0.y, l1.x, l1.y);
+        }
+    }
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t addr) {
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}\n" ::"r"(addr) : "memory");
+}
+
+// top-2 update of (m1, m2) with the pair (a, b)
+template<bool NODUP>
+__device__ __forceinline__ void top2_pair(float a, float b, float& m1, float& m2) {
+    const float hi = fmaxf(a, b);
+    if constexpr (NODUP)
+        m2 = fmaxf(fmaxf(m2, fminf(a, b)), fminf(m1, hi));
+    m1 = fmaxf(m1, hi);
+}
+
+// merge top-2 sets (m1, m2) <- (m1, m2) u (r1, r2)
+template<bool NODUP>
+__device__ __forceinline__ void top2_merge(float r1, float r2, float& m1, float& m2) {
+    if constexpr (NODUP)
+        m2 = fmaxf(fmaxf(m2, r2), fminf(m1, r1));
+    m1 = fmaxf(m1, r1);
+}
+
+// 32 dot products of columns j0..j0+31 (only the first `lim` are real):
+// keys dot - col/4096, four independent chains for ILP
+template<bool NODUP>
+__device__ __forceinline__ void reduce_chunk(const float (&v)[32], int j0, int lim, float& m1, float& m2) {
+    float c1[4], c2[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+        c1[i] = c2[i] = -INFINITY;
+#pragma unroll
+    for (int k = 0; k < 32; k += 2) {
+        float a = v[k] - (float)k * kColScale;
+        float b = v[k + 1] - (float)(k + 1) * kColScale;
+        if (lim < 32) {
+            a = k < lim ? a : -INFINITY;
+            b = k + 1 < lim ? b : -INFINITY;
+        }
+        top2_pair<NODUP>(a, b, c1[(k >> 1) & 3], c2[(k >> 1) & 3]);
+    }
+    top2_merge<NODUP>(c1[1], c2[1], c1[0], c2[0]);
+    top2_merge<NODUP>(c1[3], c2[3], c1[2], c2[2]);
+    top2_merge<NODUP>(c1[2], c2[2], c1[0], c2[0]);
+    const float off = (float)j0 * kColScale;
+    top2_merge<NODUP>(c1[0] - off, c2[0] - off, m1, m2);
+}
+
+// Warp roles of the pipelined CTA (one CTA = one row x 128 query pixels):
+//   warps 0..7   epilogue: warp w reads TMEM lane quarter w%4, columns
+//                [64*(w/4), 64*(w/4)+64) of each accumulator
+//   warps 8..11  producers: thread p expands candidate row p of each tile
+//                into the FP8 ring (and query row p into the A tile)
+//   warp 12      MMA issue (one lane)
+// Two smem B buffers and two TMEM accumulators (2 x 128 columns) let the
+// producers, the tensor core and the epilogue work on three tiles at once.
+constexpr int kEpiWarps = 8;
+constexpr int kProdWarps = 4;
+constexpr int kThreadsTC = 32 * (kEpiWarps + kProdWarps + 1);
+constexpr int kAccCols = kRows;
+
+struct TcShared {
+    uint64_t full_b[2];     // producers -> MMA, 128 arrivals
+    uint64_t acc_full[2];   // MMA commit -> epilogue / producers
+    uint64_t acc_empty[2];  // epilogue -> MMA, 256 arrivals
+    uint32_t tmem;
+    int abort;
+    float2 red[kRows];      // second column half's (m1, m2) per query
+};
+
+__device__ __forceinline__ bool wait_or_abort(uint32_t addr, uint32_t parity, volatile int* abort) {
+    const long long start = clock64();
+    while (!mbar_try_wait(addr, parity)) {
+        if (*abort)
+            return false;
+        if (clock64() - start > kWaitCycles) {
+            *abort = 1;
+            return false;
+        }
+    }
+    return true;
+}
+
+template<int NW, bool NODUP>
+__global__ void __launch_bounds__(kThreadsTC, 2) k_search_tc(const uint32_t* __restrict__ d0,
+                                                             const uint32_t* __restrict__ d1, int rows, int cols,
+                                                             int16_t* __restrict__ disp, long long disp_pitch,
+                                                             int32_t* __restrict__ best0,
+                                                             int32_t* __restrict__ best1) {
+    constexpr int KB = NW * 32;       // FP8 elements (bytes) per descriptor
+    constexpr int TILE = kRows * KB;  // bytes of one 128-row tile
+    constexpr int KSTEPS = KB / 32;   // MMA K = 32 bytes per instruction
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint8_t* sA = smem;
+    uint8_t* sB = smem + TILE;  // two buffers
+    uint2* lut = reinterpret_cast<uint2*>(smem + 3 * TILE);
+    __shared__ TcShared sh;
+    volatile int* abort = &sh.abort;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int row = blockIdx.y, dir = blockIdx.z;
+    const int m0 = blockIdx.x * kRows;
+    const size_t row_off = (size_t)row * cols * NW;
+    const uint32_t* qrow = (dir ? d1 : d0) + row_off;
+    const uint32_t* crow = (dir ? d0 : d1) + row_off;
+    const int ntiles = (cols + kRows - 1) / kRows;
+
+    for (int e = tid; e < 256; e += kThreadsTC)
+        lut[e] = make_uint2(expand_nibble(e & 0xFu), expand_nibble(e >> 4));
+    if (warp == 0) {
+        tmem_alloc(smem_u32(&sh.tmem), 2 * kAccCols);
+        tmem_relinquish();
+    }
+    if (tid == 0) {
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(smem_u32(&sh.full_b[b]), 32 * kProdWarps);
+            mbar_init(smem_u32(&sh.acc_full[b]), 1);
+            mbar_init(smem_u32(&sh.acc_empty[b]), 32 * kEpiWarps);
+        }
+        sh.abort = 0;
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = sh.tmem;
+
+    if (warp >= kEpiWarps + kProdWarps) {
+        // ---- MMA issue ----
+        if (lane == 0) {
+            const uint32_t a_addr = smem_u32(sA);
+            int issued = -1;
+            for (int t = 0; t < ntiles; ++t) {
+                const int b = t & 1;
+                if (!wait_or_abort(smem_u32(&sh.full_b[b]), (t >> 1) & 1, abort))
+                    break;
+                if (t >= 2 && !wait_or_abort(smem_u32(&sh.acc_empty[b]), ((t >> 1) - 1) & 1, abort))
+                    break;
+                fence_after();
+                const uint32_t b_addr = smem_u32(sB + b * TILE);
+#pragma unroll
+                for (int s = 0; s < KSTEPS; ++s)
+                    mma_f8(tmem + b * kAccCols, smem_desc(a_addr + s * 256, 128, 8 * KB),
+                           smem_desc(b_addr + s * 256, 128, 8 * KB), s > 0 ? 1u : 0u);
+                mma_commit(smem_u32(&sh.acc_full[b]));
+                issued = t;
+            }
+            if (issued >= 0 && *abort)  // let the last MMA land before TMEM is freed
+                wait_or_abort(smem_u32(&sh.acc_full[issued & 1]), (issued >> 1) & 1, abort);
+        }
+    } else if (warp >= kEpiWarps) {
+        // ---- producers ----
+        const int p = tid - 32 * kEpiWarps;
+        expand_row<NW>(sA, p, qrow + (size_t)min(m0 + p, cols - 1) * NW, lut);
+        for (int t = 0; t < ntiles; ++t) {
+            const int b = t & 1;
+            if (t >= 2 && !wait_or_abort(smem_u32(&sh.acc_full[b]), ((t >> 1) - 1) & 1, abort))
+                break;
+            expand_row<NW>(sB + b * TILE, p, crow + (size_t)min(t * kRows + p, cols - 1) * NW, lut);
+            fence_async_smem();
+            mbar_arrive(smem_u32(&sh.full_b[b]));
+        }
+    } else {
+        // ---- epilogue ----
+        const int q = warp & 3, half = warp >> 2;
+        const uint32_t lane_addr = tmem + ((uint32_t)(q * 32) << 16) + half * 64;
+        float m1 = -INFINITY, m2 = -INFINITY;
+        bool ok = true;
+        for (int t = 0; t < ntiles && ok; ++t) {
+            const int b = t & 1;
+            ok = wait_or_abort(smem_u32(&sh.acc_full[b]), (t >> 1) & 1, abort);
+            ok = __all_sync(0xffffffffu, ok);
+            if (!ok)
+                break;
+            fence_after();
+#pragma unroll
+            for (int ch = 0; ch < 2; ++ch) {
+                const int j0 = t * kRows + half * 64 + ch * 32;
+                if (j0 < cols) {
+                    float v[32];
+                    tmem_ld32(lane_addr + b * kAccCols + ch * 32, v);
+                    reduce_chunk<NODUP>(v, j0, cols - j0, m1, m2);
+                }
+            }
+            fence_before();
+            mbar_arrive(smem_u32(&sh.acc_empty[b]));
+        }
+        if (half == 1)
+            sh.red[q * 32 + lane] = make_float2(m1, m2);
+        asm volatile("bar.sync 1, %0;" ::"r"(32 * kEpiWarps) : "memory");
+        const int c = m0 + q * 32 + lane;
+        if (half == 0 && !*abort && c < cols) {
+            const float2 r = sh.red[q * 32 + lane];
+            top2_merge<NODUP>(r.x, r.y, m1, m2);
+            const float v1 = ceilf(m1);
+            const int best = (int)((v1 - m1) * 4096.0f);
+            const bool valid = !NODUP || ceilf(m2) != v1;
+            if (disp) {
+                int16_t* o = reinterpret_cast<int16_t*>(reinterpret_cast<char*>(disp) + row * disp_pitch);
+                o[c] = valid ? (int16_t)(c - best) : kInvalidDisp;
+            } else {
+                (dir ? best1 : best0)[(size_t)row * cols + c] = valid ? best : -1;
+            }
+        }
+    }
+
+    fence_before();
+    __syncthreads();
+    if (tid == 0 && *abort)
+        atomicAdd(&g_tc_faults, 1u);
+    if (warp == 0) {
+        fence_after();
+        tmem_dealloc(tmem, 2 * kAccCols);
+    }
+}
+
+template<int NW, bool NODUP>
+cudaError_t launch_tc_nw(const uint32_t* d0, const uint32_t* d1, int rows, int cols, int dirs, int16_t* disp,
+                         long long disp_pitch, int32_t* b0, int32_t* b1, cudaStream_t st) {
+    constexpr int TILE = kRows * NW * 32;
+    // at least 80 KB per CTA: at most 2 CTAs (2 x 256 TMEM columns) per SM
+    const size_t smem = max((size_t)3 * TILE + 256 * sizeof(uint2), (size_t)80 * 1024);
+    auto k = k_search_tc<NW, NODUP>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess)
+        return e;
+    const dim3 grid((cols + kRows - 1) / kRows, rows, dirs);
+    k<<<grid, kThreadsTC, smem, st>>>(d0, d1, rows, cols, disp, disp_pitch, b0, b1);
+    return cudaGetLastError();
+}
+
+template<bool NODUP>
+cudaError_t launch_tc_dup(const uint32_t* d0, const uint32_t* d1, int rows, int cols, int nwords, int dirs,
+                          int16_t* disp, long long disp_pitch, int32_t* b0, int32_t* b1, cudaStream_t st) {
+    switch (nwords) {
+        case 1: return launch_tc_nw<1, NODUP>(d0, d1, rows, cols, dirs, disp, disp_pitch, b0, b1, st);
+        case 2: return launch_tc_nw<2, NODUP>(d0, d1, rows, cols, dirs, disp, disp_pitch, b0, b1, st);
+        case 4: return launch_tc_nw<4, NODUP>(d0, d1, rows, cols, dirs, disp, disp_pitch, b0, b1, st);
+        case 8: return launch_tc_nw<8, NODUP>(d0, d1, rows, cols, dirs, disp, disp_pitch, b0, b1, st);
+        case 12: return launch_tc_nw<12, NODUP>(d0, d1, rows, cols, dirs, disp, disp_pitch, b0, b1, st);
+        case 16: return launch_tc_nw<16, NODUP>(d0, d1, rows, cols, dirs, disp, disp_pitch, b0, b1, st);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace
+
+bool search_tc_supported(int cols) { return cols >= 1 && cols <= kMaxCols; }
+
+cudaError_t launch_search_tc(const uint32_t* desc0, const uint32_t* desc1, int rows, int cols, int nwords,
+                             bool nodupes, int directions, int16_t* disp, long long disp_pitch, int32_t* best0,
+                             int32_t* best1, cudaStream_t st) {
+    if (!search_tc_supported(cols) || rows < 1)
+        return cudaErrorInvalidValue;
+    return nodupes ? launch_tc_dup<true>(desc0, desc1, rows, cols, nwords, directions, disp, disp_pitch, best0,
+                                         best1, st)
+                   : launch_tc_dup<false>(desc0, desc1, rows, cols, nwords, directions, disp, disp_pitch, best0,
+                                          best1, st);
+}
+
+unsigned int read_tc_faults() {
+    unsigned int v = 0;
+    cudaMemcpyFromSymbol(&v, g_tc_faults, sizeof v);
+    return v;
+}
+
+}  // namespace bicos_gb300

@@ -51,3 +51,8 @@ def test_search_single_column(cuda, oracle):
     for flags in (0, 1, 2, 3):
         got = host(lbg.search(dev(d0.view(np.int32), cuda), dev(d1.view(np.int32), cuda), flags, 0))
         assert_same(got, oracle.search(d0, d1, flags, 0))
+
+
+def test_no_kernel_wait_ran_out(cuda, native):
+    """the tensor-core search's bounded waits never expired in this process"""
+    assert native.load().bicos_kernel_faults() == 0
