@@ -65,7 +65,12 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t addr, uint32_t parity) {
 
 // canonical K-major, no swizzle: core matrix = 8 rows x 16 bytes (128 B
 // contiguous); LBO = distance of K-adjacent core matrices, SBO = distance
-// of 8-row groups; bits 46..47 = 1 (descriptor version)
+// of 8-row groups; bits 46..47 = 1 (descriptor version).  Tiles here are
+// K-chunk major: the 16 core matrices of one 16-byte K chunk (all 128 rows)
+// are contiguous (SBO = 128 B, LBO = 2 KB), so an MMA's operand fetch of
+// one K step walks contiguous shared memory instead of 16 rows 1 KB apart
+// that share their banks.
+constexpr uint32_t kChunkBytes = 128 * 16;  // one 16-byte K chunk of 128 rows
 __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
     return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
            (1ull << 46);
@@ -111,31 +116,49 @@ __device__ __forceinline__ uint32_t expand_nibble(uint32_t x) {
     return 0xB8B8B8B8u - (s << 7);
 }
 
-// one descriptor (NW words) into row rr of a 128-row FP8 tile
+// one descriptor's words, loaded ahead of its expansion
 template<int NW>
-__device__ __forceinline__ void expand_row(uint8_t* tile, int rr, const uint32_t* desc, const uint2* lut) {
-    constexpr int KB = NW * 32;
-    uint4 w4[(NW + 3) / 4];
+struct Desc {
+    uint32_t w[NW];
+};
+
+template<int NW>
+__device__ __forceinline__ Desc<NW> load_desc(const uint32_t* p) {
+    Desc<NW> d;
     if constexpr (NW % 4 == 0) {
 #pragma unroll
-        for (int j = 0; j < NW / 4; ++j)
-            w4[j] = __ldg(reinterpret_cast<const uint4*>(desc) + j);
+        for (int j = 0; j < NW / 4; ++j) {
+            const uint4 q = __ldg(reinterpret_cast<const uint4*>(p) + j);
+            d.w[4 * j] = q.x;
+            d.w[4 * j + 1] = q.y;
+            d.w[4 * j + 2] = q.z;
+            d.w[4 * j + 3] = q.w;
+        }
+    } else if constexpr (NW == 2) {
+        const uint2 q = __ldg(reinterpret_cast<const uint2*>(p));
+        d.w[0] = q.x;
+        d.w[1] = q.y;
+    } else {
+        d.w[0] = __ldg(p);
     }
-    uint8_t* base = tile + (rr >> 3) * (8 * KB) + (rr & 7) * 16;
+    return d;
+}
+
+// one descriptor into row rr of a 128-row FP8 tile (canonical layout);
+// lut: 16 words, nibble -> 4 FP8 values, one word per bank, so the
+// warp's lookups never conflict
+template<int NW>
+__device__ __forceinline__ void expand_desc(uint8_t* tile, int rr, const Desc<NW>& d, const uint32_t* lut) {
+    constexpr int KB = NW * 32;
+    uint8_t* base = tile + (rr >> 3) * 128 + (rr & 7) * 16;
 #pragma unroll
     for (int w = 0; w < NW; ++w) {
-        uint32_t x;
-        if constexpr (NW % 4 == 0) {
-            const uint4 q = w4[w >> 2];
-            x = (w & 3) == 0 ? q.x : (w & 3) == 1 ? q.y : (w & 3) == 2 ? q.z : q.w;
-        } else {
-            x = __ldg(desc + w);
-        }
+        const uint32_t x = d.w[w];
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
-            const uint2 l0 = lut[(x >> (16 * h)) & 0xFFu];
-            const uint2 l1 = lut[(x >> (16 * h + 8)) & 0xFFu];
-            *reinterpret_cast<uint4*>(base + (2 * w + h) * 128) = make_uint4(l0.x, l0.y, l1.x, l1.y);
+            const uint32_t y = x >> (16 * h);
+            *reinterpret_cast<uint4*>(base + (2 * w + h) * kChunkBytes) =
+                make_uint4(lut[y & 0xFu], lut[(y >> 4) & 0xFu], lut[(y >> 8) & 0xFu], lut[(y >> 12) & 0xFu]);
         }
     }
 }
@@ -144,26 +167,40 @@ __device__ __forceinline__ void mbar_arrive(uint32_t addr) {
     asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}\n" ::"r"(addr) : "memory");
 }
 
-// top-2 update of (m1, m2) with the pair (a, b)
-template<bool NODUP>
+// three-input max (sm_100+): one ALU instruction
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+
+// top-2 update of (m1, m2) with the pair (a, b).  min/max run on the
+// half-rate ALU pipe, so the pair's minimum is formed as (a + b) - max on
+// the FMA pipe: exact, since keys are multiples of 2^-12 below 2^10 in
+// magnitude.  MASKED pairs may hold -inf and use a plain min instead.
+template<bool NODUP, bool MASKED>
 __device__ __forceinline__ void top2_pair(float a, float b, float& m1, float& m2) {
-    const float hi = fmaxf(a, b);
-    if constexpr (NODUP)
-        m2 = fmaxf(fmaxf(m2, fminf(a, b)), fminf(m1, hi));
-    m1 = fmaxf(m1, hi);
+    if constexpr (NODUP) {
+        const float hi = fmaxf(a, b);
+        const float lo = MASKED ? fminf(a, b) : (a + b) - hi;
+        m2 = fmax3(m2, lo, fminf(m1, hi));
+        m1 = fmaxf(m1, hi);
+    } else {
+        m1 = fmax3(m1, a, b);
+    }
 }
 
 // merge top-2 sets (m1, m2) <- (m1, m2) u (r1, r2)
 template<bool NODUP>
 __device__ __forceinline__ void top2_merge(float r1, float r2, float& m1, float& m2) {
     if constexpr (NODUP)
-        m2 = fmaxf(fmaxf(m2, r2), fminf(m1, r1));
+        m2 = fmax3(m2, r2, fminf(m1, r1));
     m1 = fmaxf(m1, r1);
 }
 
-// 32 dot products of columns j0..j0+31 (only the first `lim` are real):
-// keys dot - col/4096, four independent chains for ILP
-template<bool NODUP>
+// 32 dot products of columns j0..j0+31 (MASKED: only the first `lim` are
+// real): keys dot - col/4096, four independent chains for ILP
+template<bool NODUP, bool MASKED>
 __device__ __forceinline__ void reduce_chunk(const float (&v)[32], int j0, int lim, float& m1, float& m2) {
     float c1[4], c2[4];
 #pragma unroll
@@ -173,11 +210,11 @@ __device__ __forceinline__ void reduce_chunk(const float (&v)[32], int j0, int l
     for (int k = 0; k < 32; k += 2) {
         float a = v[k] - (float)k * kColScale;
         float b = v[k + 1] - (float)(k + 1) * kColScale;
-        if (lim < 32) {
+        if constexpr (MASKED) {
             a = k < lim ? a : -INFINITY;
             b = k + 1 < lim ? b : -INFINITY;
         }
-        top2_pair<NODUP>(a, b, c1[(k >> 1) & 3], c2[(k >> 1) & 3]);
+        top2_pair<NODUP, MASKED>(a, b, c1[(k >> 1) & 3], c2[(k >> 1) & 3]);
     }
     top2_merge<NODUP>(c1[1], c2[1], c1[0], c2[0]);
     top2_merge<NODUP>(c1[3], c2[3], c1[2], c2[2]);
@@ -192,15 +229,22 @@ __device__ __forceinline__ void reduce_chunk(const float (&v)[32], int j0, int l
 //   warps 8..11  producers: thread p expands candidate row p of each tile
 //                into the FP8 ring (and query row p into the A tile)
 //   warp 12      MMA issue (one lane)
-// Two smem B buffers and two TMEM accumulators (2 x 128 columns) let the
-// producers, the tensor core and the epilogue work on three tiles at once.
+// A ring of smem B buffers (4 for words up to 128 bits, else 2) and two
+// TMEM accumulators (2 x 128 columns) let the producers run ahead of the
+// tensor core, which runs one tile ahead of the epilogue.
 constexpr int kEpiWarps = 8;
 constexpr int kProdWarps = 4;
 constexpr int kThreadsTC = 32 * (kEpiWarps + kProdWarps + 1);
 constexpr int kAccCols = kRows;
 
+constexpr int kMaxStages = 4;
+
+template<int NW>
+__host__ __device__ constexpr int b_stages() { return NW <= 4 ? 4 : 2; }
+
 struct TcShared {
-    uint64_t full_b[2];     // producers -> MMA, 128 arrivals
+    uint64_t full_b[kMaxStages];   // producers -> MMA, 128 arrivals
+    uint64_t b_empty[kMaxStages];  // MMA commit -> producers (slot read)
     uint64_t acc_full[2];   // MMA commit -> epilogue / producers
     uint64_t acc_empty[2];  // epilogue -> MMA, 256 arrivals
     uint32_t tmem;
@@ -230,10 +274,11 @@ __global__ void __launch_bounds__(kThreadsTC, 2) k_search_tc(const uint32_t* __r
     constexpr int KB = NW * 32;       // FP8 elements (bytes) per descriptor
     constexpr int TILE = kRows * KB;  // bytes of one 128-row tile
     constexpr int KSTEPS = KB / 32;   // MMA K = 32 bytes per instruction
+    constexpr int STAGES = b_stages<NW>();
     extern __shared__ __align__(1024) uint8_t smem[];
     uint8_t* sA = smem;
-    uint8_t* sB = smem + TILE;  // two buffers
-    uint2* lut = reinterpret_cast<uint2*>(smem + 3 * TILE);
+    uint8_t* sB = smem + TILE;  // STAGES buffers
+    uint32_t* lut = reinterpret_cast<uint32_t*>(smem + (1 + STAGES) * TILE);
     __shared__ TcShared sh;
     volatile int* abort = &sh.abort;
 
@@ -245,15 +290,18 @@ __global__ void __launch_bounds__(kThreadsTC, 2) k_search_tc(const uint32_t* __r
     const uint32_t* crow = (dir ? d0 : d1) + row_off;
     const int ntiles = (cols + kRows - 1) / kRows;
 
-    for (int e = tid; e < 256; e += kThreadsTC)
-        lut[e] = make_uint2(expand_nibble(e & 0xFu), expand_nibble(e >> 4));
+    if (tid < 16)
+        lut[tid] = expand_nibble(tid);
     if (warp == 0) {
         tmem_alloc(smem_u32(&sh.tmem), 2 * kAccCols);
         tmem_relinquish();
     }
     if (tid == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            mbar_init(smem_u32(&sh.full_b[s]), 32 * kProdWarps);
+            mbar_init(smem_u32(&sh.b_empty[s]), 1);
+        }
         for (int b = 0; b < 2; ++b) {
-            mbar_init(smem_u32(&sh.full_b[b]), 32 * kProdWarps);
             mbar_init(smem_u32(&sh.acc_full[b]), 1);
             mbar_init(smem_u32(&sh.acc_empty[b]), 32 * kEpiWarps);
         }
@@ -270,18 +318,19 @@ __global__ void __launch_bounds__(kThreadsTC, 2) k_search_tc(const uint32_t* __r
             const uint32_t a_addr = smem_u32(sA);
             int issued = -1;
             for (int t = 0; t < ntiles; ++t) {
-                const int b = t & 1;
-                if (!wait_or_abort(smem_u32(&sh.full_b[b]), (t >> 1) & 1, abort))
+                const int b = t & 1, slot = t % STAGES;
+                if (!wait_or_abort(smem_u32(&sh.full_b[slot]), (t / STAGES) & 1, abort))
                     break;
                 if (t >= 2 && !wait_or_abort(smem_u32(&sh.acc_empty[b]), ((t >> 1) - 1) & 1, abort))
                     break;
                 fence_after();
-                const uint32_t b_addr = smem_u32(sB + b * TILE);
+                const uint32_t b_addr = smem_u32(sB + slot * TILE);
 #pragma unroll
                 for (int s = 0; s < KSTEPS; ++s)
-                    mma_f8(tmem + b * kAccCols, smem_desc(a_addr + s * 256, 128, 8 * KB),
-                           smem_desc(b_addr + s * 256, 128, 8 * KB), s > 0 ? 1u : 0u);
+                    mma_f8(tmem + b * kAccCols, smem_desc(a_addr + s * 2 * kChunkBytes, kChunkBytes, 128),
+                           smem_desc(b_addr + s * 2 * kChunkBytes, kChunkBytes, 128), s > 0 ? 1u : 0u);
                 mma_commit(smem_u32(&sh.acc_full[b]));
+                mma_commit(smem_u32(&sh.b_empty[slot]));
                 issued = t;
             }
             if (issued >= 0 && *abort)  // let the last MMA land before TMEM is freed
@@ -289,15 +338,35 @@ __global__ void __launch_bounds__(kThreadsTC, 2) k_search_tc(const uint32_t* __r
         }
     } else if (warp >= kEpiWarps) {
         // ---- producers ----
+        // a register ring keeps the descriptors of the next PF tiles in flight
+        constexpr int PF = NW <= 4 ? 4 : 2;
         const int p = tid - 32 * kEpiWarps;
-        expand_row<NW>(sA, p, qrow + (size_t)min(m0 + p, cols - 1) * NW, lut);
-        for (int t = 0; t < ntiles; ++t) {
-            const int b = t & 1;
-            if (t >= 2 && !wait_or_abort(smem_u32(&sh.acc_full[b]), ((t >> 1) - 1) & 1, abort))
-                break;
-            expand_row<NW>(sB + b * TILE, p, crow + (size_t)min(t * kRows + p, cols - 1) * NW, lut);
-            fence_async_smem();
-            mbar_arrive(smem_u32(&sh.full_b[b]));
+        auto cand = [&](int t) {
+            return load_desc<NW>(crow + (size_t)min(min(t, ntiles - 1) * kRows + p, cols - 1) * NW);
+        };
+        Desc<NW> ring[PF];
+#pragma unroll
+        for (int i = 0; i < PF; ++i)
+            ring[i] = cand(i);
+        expand_desc<NW>(sA, p, load_desc<NW>(qrow + (size_t)min(m0 + p, cols - 1) * NW), lut);
+        bool live = true;
+        for (int t0 = 0; t0 < ntiles && live; t0 += PF) {
+#pragma unroll
+            for (int i = 0; i < PF; ++i) {
+                const int t = t0 + i;
+                if (t >= ntiles)
+                    break;
+                const Desc<NW> cur = ring[i];
+                ring[i] = cand(t + PF);
+                const int slot = t % STAGES;
+                if (t >= STAGES && !wait_or_abort(smem_u32(&sh.b_empty[slot]), (t / STAGES - 1) & 1, abort)) {
+                    live = false;
+                    break;
+                }
+                expand_desc<NW>(sB + slot * TILE, p, cur, lut);
+                fence_async_smem();
+                mbar_arrive(smem_u32(&sh.full_b[slot]));
+            }
         }
     } else {
         // ---- epilogue ----
@@ -318,7 +387,10 @@ __global__ void __launch_bounds__(kThreadsTC, 2) k_search_tc(const uint32_t* __r
                 if (j0 < cols) {
                     float v[32];
                     tmem_ld32(lane_addr + b * kAccCols + ch * 32, v);
-                    reduce_chunk<NODUP>(v, j0, cols - j0, m1, m2);
+                    if (cols - j0 >= 32)
+                        reduce_chunk<NODUP, false>(v, j0, 32, m1, m2);
+                    else
+                        reduce_chunk<NODUP, true>(v, j0, cols - j0, m1, m2);
                 }
             }
             fence_before();
@@ -358,7 +430,7 @@ cudaError_t launch_tc_nw(const uint32_t* d0, const uint32_t* d1, int rows, int c
                          long long disp_pitch, int32_t* b0, int32_t* b1, cudaStream_t st) {
     constexpr int TILE = kRows * NW * 32;
     // at least 80 KB per CTA: at most 2 CTAs (2 x 256 TMEM columns) per SM
-    const size_t smem = max((size_t)3 * TILE + 256 * sizeof(uint2), (size_t)80 * 1024);
+    const size_t smem = max((size_t)(1 + b_stages<NW>()) * TILE + 64, (size_t)80 * 1024);
     auto k = k_search_tc<NW, NODUP>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess)
