@@ -14,6 +14,8 @@
 // runs.
 #include <math.h>
 
+#include <type_traits>
+
 #include "kernels.cuh"
 
 namespace bicos_gb300 {
@@ -253,16 +255,392 @@ __global__ void __launch_bounds__(128) k_agree_subpixel(const __grid_constant__ 
     put_corr<TP>(p, row, col, corr);
 }
 
+// Single-precision subpixel sweep, same results as k_agree_subpixel<T,
+// false, NMAX>, organised for throughput:
+//  - per pixel, the frame coefficients (a, b, c) and the centred left
+//    samples d0 are staged once in shared memory as one float4 per frame
+//    (each thread reads back only its own column, so no barrier is needed);
+//  - XG consecutive sweep points per pass: one coefficient load feeds XG
+//    interpolants, the XG covariance chains are independent, and the
+//    interpolants stay in registers for the second NCC pass.  Each point's
+//    sums still run over t in order, and the best point is taken in
+//    increasing x, as the sequential sweep does;
+//  - round half to even plus the wrap to T is q + 1.5*2^23 (ulp 1 in
+//    [2^23, 2^24)), whose low mantissa bits are the two's-complement
+//    integer, masked to 8/16 bits and turned back into a float with the
+//    2^23 exponent trick: the value of (T)__float2int_rn(q) without any
+//    conversion instruction;
+constexpr int kSubThreads = 64;
+
+template<typename T>
+__device__ __forceinline__ float round_wrap_f(float q) {
+    constexpr uint32_t kMask = sizeof(T) == 1 ? 0xFFu : 0xFFFFu;
+    const float f = __fadd_rn(q, 12582912.0f);
+    return __fsub_rn(__uint_as_float((__float_as_uint(f) & kMask) | 0x4B000000u), 8388608.0f);
+}
+
+__device__ __forceinline__ float nxc_from(float cov, float var0, float var1, bool mv, float minvar) {
+    return (mv && (var0 < minvar || var1 < minvar)) ? -1.f : __fdiv_rn(cov, __fsqrt_rn(__fmul_rn(var0, var1)));
+}
+
+template<typename T, int NMAX>
+__global__ void __launch_bounds__(kSubThreads) k_subpixel_f32(const __grid_constant__ AgreeParams p) {
+    constexpr int XG = NMAX <= 33 ? 4 : 2;
+    extern __shared__ float4 coef[];  // [NMAX][kSubThreads]: a, b, c, d0
+    const int tid = threadIdx.x;
+    const int col = blockIdx.x * kSubThreads + tid;
+    const int row = blockIdx.y;
+    const int cols = p.s.cols, n = p.s.n;
+    if (col >= cols)
+        return;
+    float result = NAN, corr = NAN;
+    const int16_t d = reinterpret_cast<const int16_t*>(reinterpret_cast<const char*>(p.raw) + row * p.raw_pitch)[col];
+    const int col1 = col - d;
+    const bool mv = p.has_minvar != 0;
+    const float fn = (float)n;
+    if (d != kInvalidDisp && col1 >= 0 && col1 < cols) {
+        // two streaming passes over the frames (sums, then centred values)
+        int sx = 0, sy = 0;
+        const bool border = col1 == 0 || col1 == cols - 1;
+#pragma unroll 4
+        for (int t = 0; t < n; ++t) {
+            sx += ld_px<T>(p.s, 0, t, row, col);
+            if (border)
+                sy += ld_px<T>(p.s, 1, t, row, col1);
+        }
+        const float m0 = __fdiv_rn((float)sx, fn);
+        if (border) {
+            const float m1 = __fdiv_rn((float)sy, fn);
+            float cov = 0.f, var0 = 0.f, var1 = 0.f;
+#pragma unroll 4
+            for (int t = 0; t < n; ++t) {
+                const float d0 = __fsub_rn((float)ld_px<T>(p.s, 0, t, row, col), m0);
+                const float d1 = __fsub_rn((float)ld_px<T>(p.s, 1, t, row, col1), m1);
+                cov = __fmaf_rn(d0, d1, cov);
+                var0 = __fmaf_rn(d0, d0, var0);
+                var1 = __fmaf_rn(d1, d1, var1);
+            }
+            corr = nxc_from(cov, var0, var1, mv, p.minvar);
+            if (!(corr < p.thr))
+                result = (float)d;
+        } else {
+            float var0 = 0.f;
+#pragma unroll 4
+            for (int t = 0; t < n; ++t) {
+                const float d0 = __fsub_rn((float)ld_px<T>(p.s, 0, t, row, col), m0);
+                var0 = __fmaf_rn(d0, d0, var0);
+                const int y0 = ld_px<T>(p.s, 1, t, row, col1 - 1);
+                const int y1 = ld_px<T>(p.s, 1, t, row, col1);
+                const int y2 = ld_px<T>(p.s, 1, t, row, col1 + 1);
+                coef[t * kSubThreads + tid] =
+                    make_float4(0.5f * (float)(y0 - 2 * y1 + y2), 0.5f * (float)(y2 - y0), (float)y1, d0);
+            }
+            float best_x = 0.f, best = -1.f;
+            float xs = -1.f;
+            while (xs <= 1.f) {
+                float xv[XG];
+                bool on[XG];
+#pragma unroll
+                for (int g = 0; g < XG; ++g) {
+                    xv[g] = xs;
+                    on[g] = xs <= 1.f;
+                    xs = __fadd_rn(xs, p.step);
+                }
+                float iv[XG][NMAX];
+                float s1[XG];
+#pragma unroll
+                for (int g = 0; g < XG; ++g)
+                    s1[g] = 0.f;
+#pragma unroll
+                for (int t = 0; t < NMAX; ++t) {
+                    if (t < n) {
+                        const float4 k = coef[t * kSubThreads + tid];
+#pragma unroll
+                        for (int g = 0; g < XG; ++g) {
+                            const float q = __fadd_rn(
+                                __fadd_rn(__fmul_rn(__fmul_rn(k.x, xv[g]), xv[g]), __fmul_rn(k.y, xv[g])), k.z);
+                            iv[g][t] = round_wrap_f<T>(q);
+                            s1[g] = __fadd_rn(s1[g], iv[g][t]);
+                        }
+                    }
+                }
+                float m1[XG], cov[XG], var1[XG];
+#pragma unroll
+                for (int g = 0; g < XG; ++g) {
+                    m1[g] = __fdiv_rn(s1[g], fn);
+                    cov[g] = 0.f;
+                    var1[g] = 0.f;
+                }
+#pragma unroll
+                for (int t = 0; t < NMAX; ++t) {
+                    if (t < n) {
+                        const float d0 = coef[t * kSubThreads + tid].w;
+#pragma unroll
+                        for (int g = 0; g < XG; ++g) {
+                            const float d1 = __fsub_rn(iv[g][t], m1[g]);
+                            cov[g] = __fmaf_rn(d0, d1, cov[g]);
+                            var1[g] = __fmaf_rn(d1, d1, var1[g]);
+                        }
+                    }
+                }
+#pragma unroll
+                for (int g = 0; g < XG; ++g) {
+                    const float nxc = nxc_from(cov[g], var0, var1[g], mv, p.minvar);
+                    if (on[g] && best < nxc) {  // NaN never wins
+                        best_x = xv[g];
+                        best = nxc;
+                    }
+                }
+            }
+            corr = best;
+            if (!(best < p.thr))
+                result = __fsub_rn((float)d, best_x);
+        }
+    }
+    reinterpret_cast<float*>(reinterpret_cast<char*>(p.out) + row * p.out_pitch)[col] = result;
+    put_corr<float>(p, row, col, corr);
+}
+
+// Double-precision subpixel sweep, same results as k_agree_subpixel<T,
+// true, NMAX> (the reference's nxcorrd, include/impl/cuda/agree.cuh:35-65),
+// with FP64 work only where it can decide the result:
+//  - one pass over the sweep forms, per point, the exact integer moments
+//    Sy, Syy, Sxy of the rounded interpolants and an FP32 estimate
+//    rho_e = N / sqrt(Dx * Dy)  (N = n Sxy - Sx Sy, D = n S.. - S.^2, all
+//    exact integers), whose distance to the reference's FP64 value is below
+//    1e-6 (a few FP32 roundings of exact quantities; the FP64 two-pass
+//    value differs from the exact correlation by O(n 2^-53));
+//  - points whose estimate lies within kWin of the running best are kept
+//    (in sweep order), as are points whose min-variance test is too close
+//    to call from the exact moments; every other point is provably below
+//    the best and cannot be the reference's first maximum;
+//  - the kept points are evaluated with the reference's FP64 arithmetic in
+//    sweep order.  If more than kKeep points stay kept, the pixel falls
+//    back to the FP64 evaluation of every point.
+constexpr int kKeep = 6;
+constexpr float kWin = 1e-5f;
+
+// rounded, wrapped interpolant of sweep point x as an integer: the low
+// mantissa bits of q + 1.5*2^23 (see round_wrap_f)
+template<typename T>
+__device__ __forceinline__ int interp_i(const float4& k, float x) {
+    constexpr uint32_t kMask = sizeof(T) == 1 ? 0xFFu : 0xFFFFu;
+    const float q = __fadd_rn(__fadd_rn(__fmul_rn(__fmul_rn(k.x, x), x), __fmul_rn(k.y, x)), k.z);
+    return (int)(__float_as_uint(__fadd_rn(q, 12582912.0f)) & kMask);
+}
+
+// the reference's nxcorrd for sweep point x (left samples, as int bits, in
+// coef[].w)
+template<typename T, int NMAX>
+__device__ double nxcorrd_at(const float4* coef, int tid, int n, double m0, double var0, float x, bool mv,
+                             double minvar) {
+    long long sy = 0;
+    for (int t = 0; t < n; ++t)
+        sy += interp_i<T>(coef[t * kSubThreads + tid], x);
+    const double m1 = __ddiv_rn((double)sy, (double)n);
+    double cov = 0.0, var1 = 0.0;
+    for (int t = 0; t < n; ++t) {
+        const float4 k = coef[t * kSubThreads + tid];
+        const double d0 = __dsub_rn((double)__float_as_int(k.w), m0);
+        const double d1 = __dsub_rn((double)interp_i<T>(k, x), m1);
+        cov = __fma_rn(d0, d1, cov);
+        var1 = __fma_rn(d1, d1, var1);
+    }
+    if (mv && (var0 < minvar || var1 < minvar))
+        return -1.0;
+    return __ddiv_rn(cov, __dsqrt_rn(__dmul_rn(var0, var1)));
+}
+
+template<typename T, int NMAX>
+__global__ void __launch_bounds__(kSubThreads) k_subpixel_f64(const __grid_constant__ AgreeParams p) {
+    using Acc = typename std::conditional<sizeof(T) == 1, int, long long>::type;
+    extern __shared__ float4 coef[];  // [NMAX][kSubThreads]: a, b, c, left sample (int bits)
+    const int tid = threadIdx.x;
+    const int col = blockIdx.x * kSubThreads + tid;
+    const int row = blockIdx.y;
+    const int cols = p.s.cols, n = p.s.n;
+    if (col >= cols)
+        return;
+    float result = NAN;
+    double corr = NAN;
+    const int16_t d = reinterpret_cast<const int16_t*>(reinterpret_cast<const char*>(p.raw) + row * p.raw_pitch)[col];
+    const int col1 = col - d;
+    const bool mv = p.has_minvar != 0;
+    const double minvar = (double)p.minvar;
+    const double dn = (double)n;
+    if (d != kInvalidDisp && col1 >= 0 && col1 < cols) {
+        long long sx = 0, sxx = 0, sy = 0;
+        const bool border = col1 == 0 || col1 == cols - 1;
+        for (int t = 0; t < n; ++t) {
+            const int x = ld_px<T>(p.s, 0, t, row, col);
+            sx += x;
+            sxx += (long long)x * x;
+            if (border)
+                sy += ld_px<T>(p.s, 1, t, row, col1);
+        }
+        const double m0 = __ddiv_rn((double)sx, dn);
+        if (border) {
+            const double m1 = __ddiv_rn((double)sy, dn);
+            double cov = 0.0, var0 = 0.0, var1 = 0.0;
+            for (int t = 0; t < n; ++t) {
+                const double d0 = __dsub_rn((double)ld_px<T>(p.s, 0, t, row, col), m0);
+                const double d1 = __dsub_rn((double)ld_px<T>(p.s, 1, t, row, col1), m1);
+                cov = __fma_rn(d0, d1, cov);
+                var0 = __fma_rn(d0, d0, var0);
+                var1 = __fma_rn(d1, d1, var1);
+            }
+            corr = (mv && (var0 < minvar || var1 < minvar)) ? -1.0 : __ddiv_rn(cov, __dsqrt_rn(__dmul_rn(var0, var1)));
+            if (!(corr < (double)p.thr))
+                result = (float)d;
+        } else {
+            double var0 = 0.0;
+            for (int t = 0; t < n; ++t) {
+                const int x = ld_px<T>(p.s, 0, t, row, col);
+                const double d0 = __dsub_rn((double)x, m0);
+                var0 = __fma_rn(d0, d0, var0);
+                const int y0 = ld_px<T>(p.s, 1, t, row, col1 - 1);
+                const int y1 = ld_px<T>(p.s, 1, t, row, col1);
+                const int y2 = ld_px<T>(p.s, 1, t, row, col1 + 1);
+                coef[t * kSubThreads + tid] =
+                    make_float4(0.5f * (float)(y0 - 2 * y1 + y2), 0.5f * (float)(y2 - y0), (float)y1,
+                                __int_as_float(x));
+            }
+            // exact left moment and its min-variance decision
+            const long long dx = (long long)n * sxx - sx * sx;  // n^2 * variance
+            const double mvn = minvar * dn;                    // exact
+            auto below = [&](long long dd, bool& unsure) {
+                const double v = (double)dd;  // exact (< 2^53)
+                unsure = fabs(v - mvn) <= 1e-9 * fmax(mvn, 1.0);
+                return v < mvn;
+            };
+            bool unsure0;
+            const bool low0 = mv && below(dx, unsure0);
+            unsure0 = mv && unsure0;
+
+            float keep_x[kKeep];
+            float keep_r[kKeep];
+            bool keep_f[kKeep];
+            int nk = 0;
+            bool overflow = false;
+            float best_e = -1.f;  // running best estimate (the sweep starts at -1)
+            float xs = -1.f;
+            while (xs <= 1.f) {
+                Acc s1 = 0, s11 = 0, s01 = 0;
+                for (int t = 0; t < n; ++t) {
+                    const float4 k = coef[t * kSubThreads + tid];
+                    const Acc v = (Acc)interp_i<T>(k, xs);
+                    s1 += v;
+                    s11 += v * v;
+                    s01 += (Acc)__float_as_int(k.w) * v;
+                }
+                const long long S1 = s1, S11 = s11, S01 = s01;
+                const long long dy = (long long)n * S11 - S1 * S1;
+                const long long num = (long long)n * S01 - sx * S1;
+                bool unsure1 = false;
+                const bool low1 = mv && below(dy, unsure1);
+                unsure1 = mv && unsure1;
+                float re;
+                if (low0 || low1)
+                    re = -1.f;
+                else
+                    re = (float)num * rsqrtf((float)dx * (float)dy);  // NaN when flat
+                const bool forced = unsure0 || unsure1;
+                if (forced || re >= best_e - kWin) {
+                    if (re > best_e) {
+                        // drop kept points that fell out of the window
+                        int w = 0;
+                        for (int i = 0; i < nk; ++i)
+                            if (keep_f[i] || keep_r[i] >= re - kWin) {
+                                keep_x[w] = keep_x[i];
+                                keep_r[w] = keep_r[i];
+                                keep_f[w] = keep_f[i];
+                                ++w;
+                            }
+                        nk = w;
+                        if (!forced)
+                            best_e = re;
+                    }
+                    if (nk < kKeep) {
+                        keep_x[nk] = xs;
+                        keep_r[nk] = re;
+                        keep_f[nk] = forced;
+                        ++nk;
+                    } else {
+                        overflow = true;
+                    }
+                }
+                xs = __fadd_rn(xs, p.step);
+            }
+
+            double best = -1.0;
+            float best_x = 0.f;
+            if (!overflow) {
+                for (int i = 0; i < nk; ++i) {
+                    if (!keep_f[i] && keep_r[i] < best_e - kWin)
+                        continue;
+                    const double r = nxcorrd_at<T, NMAX>(coef, tid, n, m0, var0, keep_x[i], mv, minvar);
+                    if (best < r) {
+                        best = r;
+                        best_x = keep_x[i];
+                    }
+                }
+            } else {
+                for (float x = -1.f; x <= 1.f; x = __fadd_rn(x, p.step)) {
+                    const double r = nxcorrd_at<T, NMAX>(coef, tid, n, m0, var0, x, mv, minvar);
+                    if (best < r) {
+                        best = r;
+                        best_x = x;
+                    }
+                }
+            }
+            corr = best;
+            if (!(best < (double)p.thr))
+                result = __fsub_rn((float)d, best_x);
+        }
+    }
+    reinterpret_cast<float*>(reinterpret_cast<char*>(p.out) + row * p.out_pitch)[col] = result;
+    put_corr<double>(p, row, col, corr);
+}
+
+template<typename T, int NM>
+cudaError_t launch_subpixel_f64(const AgreeParams& p, cudaStream_t st) {
+    const size_t smem = (size_t)NM * kSubThreads * sizeof(float4);
+    auto k = k_subpixel_f64<T, NM>;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess)
+            return e;
+    }
+    const dim3 grid((p.s.cols + kSubThreads - 1) / kSubThreads, p.s.rows);
+    k<<<grid, kSubThreads, smem, st>>>(p);
+    return cudaGetLastError();
+}
+
+template<typename T, int NM>
+cudaError_t launch_subpixel_f32(const AgreeParams& p, cudaStream_t st) {
+    const size_t smem = (size_t)NM * kSubThreads * sizeof(float4);
+    auto k = k_subpixel_f32<T, NM>;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess)
+            return e;
+    }
+    const dim3 grid((p.s.cols + kSubThreads - 1) / kSubThreads, p.s.rows);
+    k<<<grid, kSubThreads, smem, st>>>(p);
+    return cudaGetLastError();
+}
+
 template<typename T, bool DBL, bool SUB>
 cudaError_t launch_t(const AgreeParams& p, cudaStream_t st) {
     const dim3 grid((p.s.cols + 127) / 128, p.s.rows);
     const int n = p.s.n;
-#define BICOS_AGREE_CASE(NM)                                              \
+#define BICOS_AGREE_CASE(NM)                                         \
     if (n <= NM) {                                                        \
+        if (SUB && !DBL)                                                  \
+            return launch_subpixel_f32<T, NM>(p, st);                     \
         if (SUB)                                                          \
-            k_agree_subpixel<T, DBL, NM><<<grid, 128, 0, st>>>(p);        \
-        else                                                              \
-            k_agree<T, DBL, NM><<<grid, 128, 0, st>>>(p);                 \
+            return launch_subpixel_f64<T, NM>(p, st);                     \
+        k_agree<T, DBL, NM><<<grid, 128, 0, st>>>(p);                     \
         return cudaGetLastError();                                        \
     }
     BICOS_AGREE_CASE(8)
