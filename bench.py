@@ -156,16 +156,57 @@ def peaks():
         return 6800.0, 1900.0, "fallback"
 
 
-def profile_traffic():
-    """DRAM bytes per launch of the search kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "search_mv1936_n33.md")
-    try:
-        for line in open(path):
-            if line.startswith("traffic_bytes_per_launch:"):
-                return float(line.split(":", 1)[1].split()[0])
-    except OSError:
-        pass
+def profile_traffic(kernel):
+    """DRAM bytes per launch of `kernel` from the committed ncu summaries
+    (a line "traffic_bytes_per_launch <kernel>: <bytes>")."""
+    key = f"traffic_bytes_per_launch {kernel}:"
+    for name in sorted(os.listdir(os.path.join(ROOT, "profiles"))):
+        try:
+            for line in open(os.path.join(ROOT, "profiles", name)):
+                if line.startswith(key):
+                    return float(line.split(":", 1)[1].split()[0])
+        except OSError:
+            pass
     return None
+
+
+def stage_rooflines(stages, rows, cols, n, clk):
+    """Roofline of each stage from its live CUDA-event time (ms per launch).
+
+    transform: HBM bytes 2*px*n + 2*px*16 (u8 stack in, 128-bit words out)
+    search:    tensor-core work 2*rows*cols^2*128 FLOP (+-1 FP8 dot products,
+               one direction), against the FP8 dense rate taken as twice the
+               measured bf16 GEMM rate
+    subpixel:  FP32 work of the sweep, 14 flops per (valid pixel, sweep
+               point, frame) with 20 points at step 0.1, against the FP32
+               vector peak 152 SMs x 128 lanes x 2 x SM clock
+    """
+    hbm, bf16, src = peaks()
+    px = rows * cols
+    sm_mhz = clk.get("sm_mhz") or 2070.0
+    t_tf, t_se, t_ag = [max(x, 1e-9) for x in stages]
+    tf_bytes = 2 * px * n + 2 * px * 16
+    se_flop = 2.0 * rows * cols * cols * 128
+    ag_flop = 14.0 * 0.8 * px * 20 * n  # about 80 % of pixels reach the sweep
+    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+    fp8_peak = 2 * bf16
+    return {
+        "transform": {"kernel": "k_transform_limited", "bound": "hbm", "ms": round(t_tf, 4),
+                      "achieved": round(tf_bytes / (t_tf * 1e-3) / 1e9, 1), "peak": hbm, "unit": "GB/s",
+                      "frac": round(tf_bytes / (t_tf * 1e-3) / 1e9 / hbm, 4),
+                      "peak_source": f"{src} HBM copy bandwidth",
+                      "traffic": profile_traffic("k_transform_limited"), "algorithmic_bytes": tf_bytes},
+        "search": {"kernel": "k_search_tc", "bound": "tensor", "ms": round(t_se, 4),
+                   "achieved": round(se_flop / (t_se * 1e-3) / 1e12, 1), "peak": round(fp8_peak, 1),
+                   "unit": "TFLOP/s", "frac": round(se_flop / (t_se * 1e-3) / 1e12 / fp8_peak, 4),
+                   "peak_source": f"FP8 dense = 2 x {src} bf16 GEMM rate",
+                   "traffic": profile_traffic("k_search_tc"), "algorithmic_flop": se_flop},
+        "subpixel": {"kernel": "k_subpixel_f32", "bound": "fp32", "ms": round(t_ag, 4),
+                     "achieved": round(ag_flop / (t_ag * 1e-3) / 1e12, 2), "peak": round(fp32_peak, 1),
+                     "unit": "TFLOP/s", "frac": round(ag_flop / (t_ag * 1e-3) / 1e12 / fp32_peak, 4),
+                     "peak_source": f"FP32 vector peak at the median SM clock {sm_mhz:.0f} MHz",
+                     "traffic": profile_traffic("k_subpixel_f32"), "algorithmic_flop": ag_flop},
+    }
 
 
 def run_ours(args):
@@ -209,8 +250,9 @@ def run_ours(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
 
-    def timed(double, steps, warmup, stage_times=False):
+    def timed(double, steps, warmup, stage_times=False, form=0):
         cfg = cfg_of(double)
+        cfg.nxcorr_form = form
         out = lbg.match_device(left, right, cfg)
         for _ in range(warmup):
             lbg.match_device(left, right, cfg, out=out)
@@ -259,24 +301,10 @@ def run_ours(args):
                           "agree_subpixel": round(stages[2], 4)}
     result["gpu_launches"] = 3 * args.steps
 
-    # dominant kernel roofline: the Hamming search
-    hbm, tf, src = peaks()
-    nw = 4
-    search_ms = stages[1]
-    word_ops = rows * cols * cols * nw  # 32-bit XOR+POPC word-ops per launch
-    algo_bytes = 2 * px * nw * 4 + px * 2
-    sm_clock = clk["sm_mhz"] or 1900.0
-    popc_peak = 16 * 152 * sm_clock * 1e6 / 1e9  # POPC results/clk/SM x SMs x clock, Gop/s
-    achieved = word_ops / (search_ms * 1e-3) / 1e9
-    traffic = profile_traffic()
-    result["roofline"] = {
-        "kernel": "k_search (popcount Hamming arg-min)", "bound": "int-popc",
-        "achieved": round(achieved, 1), "peak": round(popc_peak, 1), "unit": "Gop/s",
-        "frac": round(achieved / popc_peak, 4),
-        "peak_source": f"16 POPC/clk/SM x 152 SMs x median SM clock {sm_clock:.0f} MHz",
-        "traffic": traffic, "algorithmic_bytes": algo_bytes,
-        "hbm_frac_of_" + src: round(algo_bytes / (search_ms * 1e-3) / 1e9 / hbm, 5),
-    }
+    # per-stage rooflines; the headline one is the stage that takes longest
+    result["stage_rooflines"] = stage_rooflines(stages, rows, cols, n, clk)
+    dom = max(result["stage_rooflines"], key=lambda k: result["stage_rooflines"][k]["ms"])
+    result["roofline"] = dict(result["stage_rooflines"][dom], stage=dom)
 
     if not args.no_double:
         ms_d, st_d, _ = timed(True, max(1, args.steps // 2), 2, stage_times=True)
@@ -284,6 +312,13 @@ def run_ours(args):
                             "ms_per_step": round(ms_d, 4),
                             "stage_ms": {"transform": round(st_d[0], 4), "search": round(st_d[1], 4),
                                          "agree_subpixel": round(st_d[2], 4)}}
+        # the moment form (extension): exact integer moments, Sxy on the
+        # tensor cores, closed-form sweep of the unrounded interpolant, FP64
+        ms_m, st_m, _ = timed(True, max(1, args.steps // 2), 2, stage_times=True, form=1)
+        result["moment_form_double"] = {
+            "value": round(ws * px / (ms_m * 1e-3) / 1e6, 3), "unit": "Mpx/s", "ms_per_step": round(ms_m, 4),
+            "stage_ms": {"transform": round(st_m[0], 4), "search": round(st_m[1], 4),
+                         "agree_subpixel": round(st_m[2], 4)}}
 
     if not args.no_e2e:
         # host path: pinned host stacks -> bicos_match_host_v1 (upload, match, download)

@@ -91,7 +91,17 @@ typedef struct bicos_config {
     int32_t no_dupes;         /* Consistency only, default 0 */
     int32_t max_bits;         /* descriptor width limit: 256 as the reference;
                                  up to 512 accepts FULL stacks of n <= 23 (extension) */
+    int32_t nxcorr_form;      /* BICOS_NXCORR_REFERENCE (default) or BICOS_NXCORR_MOMENTS */
 } bicos_config;
+
+/* NCC forms.  REFERENCE: the reference's two-pass NCC, bit-identical
+ * results.  MOMENTS (extension, no counterpart in the reference): the
+ * correlation from exact integer moments, with the Sxy band formed on the
+ * tensor cores and the subpixel interpolant left unrounded, so the sweep's
+ * correlation is a closed-form function of the position; FP64 (precision
+ * double) or FP32 evaluates only the final polynomials and ratio.  Results
+ * differ from the reference's by the rounding of its interpolants. */
+enum { BICOS_NXCORR_REFERENCE = 0, BICOS_NXCORR_MOMENTS = 1 };
 
 /* Fills the reference defaults (include/common.hpp:73-82). */
 bicos_status bicos_config_default(bicos_config* cfg);

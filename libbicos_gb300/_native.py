@@ -30,6 +30,7 @@ class Config(C.Structure):
         ("has_min_variance", C.c_int32), ("min_variance", C.c_float),
         ("mode", C.c_int32), ("precision", C.c_int32), ("variant", C.c_int32),
         ("max_lr_diff", C.c_int32), ("no_dupes", C.c_int32), ("max_bits", C.c_int32),
+        ("nxcorr_form", C.c_int32),
     ]
 
 

@@ -219,6 +219,7 @@ bicos_status bicos_config_default(bicos_config* c) {
     c->max_lr_diff = 1;
     c->no_dupes = 0;
     c->max_bits = 256;
+    c->nxcorr_form = BICOS_NXCORR_REFERENCE;
     return BICOS_OK;
 }
 
@@ -237,7 +238,7 @@ int32_t bicos_descriptor_words(uint32_t n, int32_t mode, int32_t max_bits) {
     return words_for((int)n, mode == BICOS_MODE_FULL, max_bits);
 }
 
-int32_t bicos_kernel_faults(void) { return (int32_t)read_tc_faults(); }
+int32_t bicos_kernel_faults(void) { return (int32_t)(read_tc_faults() + read_moment_faults()); }
 
 bicos_status bicos_stage_timing(int32_t enable) {
     std::lock_guard<std::mutex> lk(g_timing.mu);
@@ -364,7 +365,22 @@ bicos_status bicos_match_v1(const bicos_image* stack0, const bicos_image* stack1
         ap.minvar = cfg->has_min_variance ? cfg->min_variance * (float)n : 0.f;  // src/impl/cpu.cpp:123
         ap.corr = corrmap ? corrmap->data : nullptr;
         ap.corr_pitch = corrmap ? (long long)corrmap->step : 0;
-        if (sub) {
+        if (cfg->nxcorr_form == BICOS_NXCORR_MOMENTS) {
+            MomentParams mp;
+            std::memset(&mp, 0, sizeof mp);
+            mp.s = ap.s;
+            mp.raw = raw;
+            mp.raw_pitch = raw_pitch;
+            mp.out = sub ? disparity->data : raw;
+            mp.out_pitch = sub ? (long long)disparity->step : raw_pitch;
+            mp.corr = ap.corr;
+            mp.corr_pitch = ap.corr_pitch;
+            mp.thr = ap.thr;
+            mp.step = ap.step;
+            mp.has_minvar = ap.has_minvar;
+            mp.minvar = ap.minvar;
+            e = launch_moments(mp, sub ? 1 : 0, dbl, st);
+        } else if (sub) {
             ap.raw = raw;
             ap.raw_pitch = raw_pitch;
             ap.out = disparity->data;

@@ -39,6 +39,25 @@ struct AgreeParams {
     float minvar;
 };
 
+// moment form of the NCC stage (moments.cu)
+struct MomentParams {
+    StackParams s;
+    const int16_t* raw;  // int16 disparity in
+    long long raw_pitch;
+    void* out;           // mode 0: int16 disparity (may alias raw), 1: float, 2: float[8] features
+    long long out_pitch;
+    void* corr;          // float / double corrmap (modes 0, 1), may be null
+    long long corr_pitch;
+    float thr;
+    float step;
+    int has_minvar;
+    float minvar;
+};
+
+// mode 0: agree at the integer disparity, 1: subpixel sweep, 2: features
+cudaError_t launch_moments(const MomentParams& p, int mode, bool dbl, cudaStream_t st);
+unsigned int read_moment_faults();
+
 cudaError_t launch_transform(const StackParams& p, int sides, bool full, int nwords,
                              uint32_t* desc0, uint32_t* desc1, cudaStream_t st);
 

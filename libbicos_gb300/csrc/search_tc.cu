@@ -16,6 +16,7 @@
 // bounded: a wait that runs out records a fault, and the CTA frees its TMEM
 // and exits.
 #include "kernels.cuh"
+#include "tcgen05.cuh"
 
 namespace bicos_gb300 {
 
@@ -23,92 +24,17 @@ __device__ unsigned int g_tc_faults = 0;
 
 namespace {
 
+using namespace tc;
+
 constexpr int kRows = 128;          // MMA M = N = 128
 constexpr float kColScale = 1.0f / 4096.0f;
 constexpr int kMaxCols = 4096;      // key exactness bound
-constexpr long long kWaitCycles = 4LL << 30;
 
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ void tmem_alloc(uint32_t dst_smem, uint32_t ncols) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(dst_smem), "r"(ncols)
-                 : "memory");
-}
-__device__ __forceinline__ void tmem_relinquish() {
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-}
-__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
-}
-__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-
-__device__ __forceinline__ void mbar_init(uint32_t addr, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(addr), "r"(count) : "memory");
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint32_t addr, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}\n"
-        : "=r"(ok)
-        : "r"(addr), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-// canonical K-major, no swizzle: core matrix = 8 rows x 16 bytes (128 B
-// contiguous); LBO = distance of K-adjacent core matrices, SBO = distance
-// of 8-row groups; bits 46..47 = 1 (descriptor version).  Tiles here are
-// K-chunk major: the 16 core matrices of one 16-byte K chunk (all 128 rows)
-// are contiguous (SBO = 128 B, LBO = 2 KB), so an MMA's operand fetch of
-// one K step walks contiguous shared memory instead of 16 rows 1 KB apart
-// that share their banks.
+// K-chunk major tiles: the 16 core matrices of one 16-byte K chunk (all 128
+// rows) are contiguous (SBO = 128 B, LBO = 2 KB), so an MMA's operand fetch
+// of one K step walks contiguous shared memory.
 constexpr uint32_t kChunkBytes = 128 * 16;  // one 16-byte K chunk of 128 rows
-__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
-    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
-           (1ull << 46);
-}
-
-// kind::f8f6f4: D f32 (bits 4-5 = 1), A/B e4m3 (0), K-major, N>>3 at 17, M>>4 at 24
-constexpr uint32_t kIdesc = (1u << 4) | ((uint32_t)(kRows >> 3) << 17) | ((uint32_t)(kRows >> 4) << 24);
-
-__device__ __forceinline__ void mma_f8(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "setp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
-        "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate)
-        : "memory");
-}
-
-__device__ __forceinline__ void mma_commit(uint32_t mbar) {
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
-                 : "memory");
-}
-
-// 32 consecutive FP32 columns of this warp's TMEM lane quarter
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
-    uint32_t r[32];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int k = 0; k < 32; ++k)
-        v[k] = __uint_as_float(r[k]);
-}
+constexpr uint32_t kIdesc = tc::idesc_f8_e4m3(kRows, kRows);
 
 // 8 descriptor bits -> 8 FP8 values (+1 set, -1 clear)
 __device__ __forceinline__ uint32_t expand_nibble(uint32_t x) {
@@ -149,7 +75,6 @@ __device__ __forceinline__ Desc<NW> load_desc(const uint32_t* p) {
 // warp's lookups never conflict
 template<int NW>
 __device__ __forceinline__ void expand_desc(uint8_t* tile, int rr, const Desc<NW>& d, const uint32_t* lut) {
-    constexpr int KB = NW * 32;
     uint8_t* base = tile + (rr >> 3) * 128 + (rr & 7) * 16;
 #pragma unroll
     for (int w = 0; w < NW; ++w) {
@@ -161,10 +86,6 @@ __device__ __forceinline__ void expand_desc(uint8_t* tile, int rr, const Desc<NW
                 make_uint4(lut[y & 0xFu], lut[(y >> 4) & 0xFu], lut[(y >> 8) & 0xFu], lut[(y >> 12) & 0xFu]);
         }
     }
-}
-
-__device__ __forceinline__ void mbar_arrive(uint32_t addr) {
-    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}\n" ::"r"(addr) : "memory");
 }
 
 // three-input max (sm_100+): one ALU instruction
@@ -252,19 +173,6 @@ struct TcShared {
     float2 red[kRows];      // second column half's (m1, m2) per query
 };
 
-__device__ __forceinline__ bool wait_or_abort(uint32_t addr, uint32_t parity, volatile int* abort) {
-    const long long start = clock64();
-    while (!mbar_try_wait(addr, parity)) {
-        if (*abort)
-            return false;
-        if (clock64() - start > kWaitCycles) {
-            *abort = 1;
-            return false;
-        }
-    }
-    return true;
-}
-
 template<int NW, bool NODUP>
 __global__ void __launch_bounds__(kThreadsTC, 2) k_search_tc(const uint32_t* __restrict__ d0,
                                                              const uint32_t* __restrict__ d1, int rows, int cols,
@@ -327,8 +235,9 @@ __global__ void __launch_bounds__(kThreadsTC, 2) k_search_tc(const uint32_t* __r
                 const uint32_t b_addr = smem_u32(sB + slot * TILE);
 #pragma unroll
                 for (int s = 0; s < KSTEPS; ++s)
-                    mma_f8(tmem + b * kAccCols, smem_desc(a_addr + s * 2 * kChunkBytes, kChunkBytes, 128),
-                           smem_desc(b_addr + s * 2 * kChunkBytes, kChunkBytes, 128), s > 0 ? 1u : 0u);
+                    mma_f8f6f4(tmem + b * kAccCols, smem_desc(a_addr + s * 2 * kChunkBytes, kChunkBytes, 128),
+                           smem_desc(b_addr + s * 2 * kChunkBytes, kChunkBytes, 128), kIdesc,
+                               s > 0 ? 1u : 0u);
                 mma_commit(smem_u32(&sh.acc_full[b]));
                 mma_commit(smem_u32(&sh.b_empty[slot]));
                 issued = t;

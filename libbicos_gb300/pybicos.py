@@ -102,6 +102,9 @@ class Config:
         self.mode = TransformMode.Limited
         self.precision = Precision.Single
         self.variant = Variant.NoDuplicates()
+        # extension (not in the reference): 0 = the reference's two-pass NCC,
+        # 1 = the moment form (tensor-core Sxy, unrounded subpixel interpolant)
+        self.nxcorr_form = 0
 
     nxcorr_threshold = property(lambda s: s._thr, lambda s, v: setattr(s, "_thr", _f32(v)))
     subpixel_step = property(lambda s: s._step, lambda s, v: setattr(s, "_step", _f32(v)))
@@ -124,6 +127,9 @@ class Config:
             raise TypeError("mode must be a TransformMode and precision a Precision")
         c.mode = self.mode.value
         c.precision = self.precision.value
+        if self.nxcorr_form not in (0, 1):
+            raise ValueError("nxcorr_form must be 0 (reference) or 1 (moments)")
+        c.nxcorr_form = int(self.nxcorr_form)
         if isinstance(self.variant, _Consistency):
             c.variant = 1
             c.max_lr_diff = self.variant.max_lr_diff

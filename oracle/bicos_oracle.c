@@ -549,3 +549,148 @@ int orc_match(const void* s0, const void* s1, int elem_bytes, int n, int rows, i
     }
     return ORC_OK;
 }
+
+/* ---- moment form (the library's extension; restates moments.cu) ---- */
+
+typedef struct {
+    const int16_t* disp;
+    const void *s0, *s1;
+    int elem_bytes, n, rows, cols;
+    float thr, step;
+    int has_minvar;
+    float minvar;
+    int dbl, mode;
+    void* out;
+    void* corr;
+} mom_ctx;
+
+/* correlation ratio p / sqrt(v0 * q), rounded as in the kernel */
+static double mom_ratio(int dbl, double p, double v0, double q) {
+    if (dbl)
+        return p / sqrt(v0 * q);
+    return (double)((float)p / sqrtf((float)v0 * (float)q));
+}
+
+static double mom_fma(int dbl, double a, double b, double c) {
+    return dbl ? fma(a, b, c) : (double)fmaf((float)a, (float)b, (float)c);
+}
+
+/* conversion of an exact int64 to the working precision */
+static double mom_cvt(int dbl, long long v) {
+    return dbl ? (double)v : (double)(float)v;
+}
+
+static void moments_rows(void* p, int r0, int r1) {
+    mom_ctx* c = (mom_ctx*)p;
+    const size_t plane = (size_t)c->rows * c->cols;
+    const long long nn = c->n;
+    for (int r = r0; r < r1; ++r)
+        for (int col = 0; col < c->cols; ++col) {
+            const size_t px = (size_t)r * c->cols + col;
+            const int16_t d = c->disp[px];
+            const int col1 = col - d;
+            const int valid = d != INVALID_I16 && col1 >= 0 && col1 < c->cols;
+            double corr = NAN;
+            float fout = NAN;
+            int16_t iout = INVALID_I16;
+            if (valid) {
+                long long sx = 0, sxx = 0, sy[5] = {0}, sxy[5] = {0}, syy[5][5] = {{0}};
+                for (int t = 0; t < c->n; ++t) {
+                    const long long x = load_px(c->s0, c->elem_bytes, t * plane + px);
+                    long long y[5];
+                    sx += x;
+                    sxx += x * x;
+                    for (int j = 0; j < 5; ++j) {
+                        const int cc = col1 + j - 2;
+                        y[j] = (cc >= 0 && cc < c->cols) ? load_px(c->s1, c->elem_bytes, t * plane + (size_t)r * c->cols + cc) : 0;
+                        sy[j] += y[j];
+                        sxy[j] += x * y[j];
+                    }
+                    for (int j = 0; j < 5; ++j)
+                        for (int k = j; k < 5; ++k)
+                            syy[j][k] += y[j] * y[k];
+                }
+                const long long v0 = nn * sxx - sx * sx;
+                const double mvn = c->dbl ? (double)c->minvar * (double)c->n
+                                          : (double)((float)c->minvar * (float)c->n);
+                const double V0 = mom_cvt(c->dbl, v0);
+                const int low0 = c->has_minvar && V0 < mvn;
+                const int border = col1 == 0 || col1 == c->cols - 1;
+                if (c->mode == 0 || border) {
+                    const long long v1 = nn * syy[2][2] - sy[2] * sy[2];
+                    const double V1 = mom_cvt(c->dbl, v1);
+                    if (c->has_minvar && (low0 || V1 < mvn))
+                        corr = -1.0;
+                    else
+                        corr = mom_ratio(c->dbl, mom_cvt(c->dbl, nn * sxy[2] - sx * sy[2]), V0, V1);
+                    const int pass = !(c->dbl ? corr < (double)c->thr : (float)corr < c->thr);
+                    if (pass) {
+                        iout = d;
+                        fout = (float)d;
+                    }
+                } else {
+                    const long long XA = sxy[1] - 2 * sxy[2] + sxy[3], XB = sxy[3] - sxy[1], XC = sxy[2];
+                    const long long YA = sy[1] - 2 * sy[2] + sy[3], YB = sy[3] - sy[1], YC = sy[2];
+                    const long long Smm = syy[1][1], Szz = syy[2][2], Sqq = syy[3][3], Smz = syy[1][2],
+                                    Szq = syy[2][3], Smq = syy[1][3];
+                    const long long AA = Smm + 4 * Szz + Sqq - 4 * Smz - 4 * Szq + 2 * Smq;
+                    const long long AB = Sqq - Smm + 2 * Smz - 2 * Szq;
+                    const long long BB = Sqq - 2 * Smq + Smm;
+                    const long long AC2 = Smz - 2 * Szz + Szq;
+                    const long long BC2 = Szq - Smz;
+                    const long long CC = Szz;
+                    const int D = c->dbl;
+                    const double P2 = mom_cvt(D, nn * XA - sx * YA), P1 = mom_cvt(D, nn * XB - sx * YB),
+                                 P0 = mom_cvt(D, 2 * (nn * XC - sx * YC));
+                    const double Q4 = mom_cvt(D, nn * AA - YA * YA), Q3 = mom_cvt(D, 2 * (nn * AB - YA * YB)),
+                                 Q2 = mom_cvt(D, nn * BB + 4 * nn * AC2 - YB * YB - 4 * YA * YC),
+                                 Q1 = mom_cvt(D, 4 * (nn * BC2 - YB * YC)), Q0 = mom_cvt(D, 4 * (nn * CC - YC * YC));
+                    const double mvq = D ? 4.0 * mvn : (double)(4.0f * (float)mvn);
+                    double best = -1.0;
+                    float best_x = 0.f;
+                    for (float xs = -1.f; xs <= 1.f; xs += c->step) {
+                        const double X = xs;
+                        const double Pv = mom_fma(D, mom_fma(D, P2, X, P1), X, P0);
+                        const double Qv = mom_fma(D, mom_fma(D, mom_fma(D, mom_fma(D, Q4, X, Q3), X, Q2), X, Q1), X, Q0);
+                        const double rr = (low0 || (c->has_minvar && Qv < mvq)) ? -1.0 : mom_ratio(D, Pv, V0, Qv);
+                        const int better = D ? best < rr : (float)best < (float)rr;
+                        if (better) {
+                            best = rr;
+                            best_x = xs;
+                        }
+                    }
+                    corr = best;
+                    const int pass = !(D ? best < (double)c->thr : (float)best < c->thr);
+                    if (pass)
+                        fout = (float)d - best_x;
+                }
+            }
+            if (c->mode == 0)
+                ((int16_t*)c->out)[px] = iout;
+            else
+                ((float*)c->out)[px] = fout;
+            if (c->corr) {
+                if (c->dbl)
+                    ((double*)c->corr)[px] = corr;
+                else
+                    ((float*)c->corr)[px] = (float)corr;
+            }
+        }
+}
+
+void orc_moments(const int16_t* disp, const void* s0, const void* s1, int elem_bytes, int n, int rows, int cols,
+                 float thr, float step, int has_minvar, float minvar, int dbl, int mode, void* out, void* corr,
+                 int nthreads) {
+    mom_ctx c = {disp, s0, s1, elem_bytes, n, rows, cols, thr, step, has_minvar, minvar, dbl, mode, out, corr};
+    if (mode == 0 && out == (void*)disp) {
+        /* in place: work from a copy of the input disparity */
+        const size_t px = (size_t)rows * cols;
+        int16_t* copy = (int16_t*)malloc(px * sizeof(int16_t));
+        memcpy(copy, disp, px * sizeof(int16_t));
+        c.disp = copy;
+        parallel_rows(rows, nthreads, moments_rows, &c);
+        free(copy);
+        return;
+    }
+    parallel_rows(rows, nthreads, moments_rows, &c);
+}

@@ -74,6 +74,16 @@ void orc_agree_subpixel(const int16_t* disp, const void* s0, const void* s1,
 float orc_nxcorr_f(const float* x, const float* y, int n, int has_minvar, float minvar);
 double orc_nxcorr_d(const double* x, const double* y, int n, int has_minvar, double minvar);
 
+/* Moment form of the agreement stage (the library's extension, no
+ * counterpart in the reference): exact integer moments and the closed-form
+ * correlation of the unrounded quadratic interpolant, evaluated with the
+ * same operations as the CUDA kernel (moments.cu).  mode 0: agree at the
+ * integer disparity, out int16 (in place allowed); mode 1: subpixel sweep,
+ * out float.  corr: float or double per dbl, may be NULL. */
+void orc_moments(const int16_t* disp, const void* s0, const void* s1, int elem_bytes, int n, int rows,
+                 int cols, float thr, float step, int has_minvar, float minvar, int dbl, int mode,
+                 void* out, void* corr, int nthreads);
+
 /* whole pipeline, src/impl/cpu.cpp:96-155 (+ the CUDA build's precision
  * switch).  disp_out: int16 (no step) or float32 (step); corr_out: float32
  * or float64 per precision, may be NULL.  Returns ORC_* and fills err. */

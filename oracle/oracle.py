@@ -262,3 +262,25 @@ def nxcorr_d(x, y, min_var=None):
     y = np.ascontiguousarray(y, np.float64)
     return lib().orc_nxcorr_d(_p(x), _p(y), len(x), int(min_var is not None),
                               float(min_var or 0.0))
+
+
+def moments(disp, stack0, stack1, thr, step=None, min_var_scaled=None, double=True, nthreads=0):
+    """Moment form of the agreement (the library's extension): returns
+    (int16 disparity, corrmap) without a step, (float disparity, corrmap)
+    with one."""
+    s0, s1 = _stack(stack0), _stack(stack1)
+    n, rows, cols = s0.shape
+    d = np.ascontiguousarray(disp, np.int16)
+    mode = 0 if step is None else 1
+    out = np.empty((rows, cols), np.int16 if mode == 0 else np.float32)
+    corr = np.empty((rows, cols), np.float64 if double else np.float32)
+    hm = min_var_scaled is not None
+    L = lib()
+    if not getattr(L, "_mom_sig", False):
+        L.orc_moments.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
+                                  C.c_float, C.c_float, C.c_int, C.c_float, C.c_int, C.c_int, C.c_void_p,
+                                  C.c_void_p, C.c_int]
+        L._mom_sig = True
+    L.orc_moments(_p(d), _p(s0), _p(s1), s0.dtype.itemsize, n, rows, cols, thr, step or 0.0, int(hm),
+                  float(min_var_scaled or 0.0), int(double), mode, _p(out), _p(corr), nthreads)
+    return out, corr
