@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-double", action="store_true")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned subpixel form")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target CPU work of the baseline sample")
     return ap.parse_args()
 
@@ -209,6 +210,25 @@ def stage_rooflines(stages, rows, cols, n, clk):
     }
 
 
+def learned_error(lbg, pybicos, left, right, plain, learned, n):
+    """RMS subpixel error (px) of the learned form and of the plain step-0.1
+    sweep against the reference sweep with step 0.01 in double precision,
+    on interior pixels valid in all three."""
+    import torch
+    c = pybicos.Config()
+    c.nxcorr_threshold = None
+    raw, _ = lbg.match_device(left, right, c)
+    ref, _ = lbg.agree_subpixel(raw, left, right, THRESHOLD, 0.01, MIN_VAR * n, double=True)
+    cols = raw.shape[1]
+    col1 = torch.arange(cols, device=raw.device)[None, :] - raw.to(torch.int32)
+    m = torch.isfinite(ref) & torch.isfinite(plain) & torch.isfinite(learned) & (col1 > 0) & (col1 < cols - 1)
+
+    def rms(v):
+        return round(float(torch.sqrt(torch.mean((v[m].double() - ref[m].double()) ** 2))), 5)
+    return {"reference": "reference sweep, step 0.01, double precision, same threshold and min_variance",
+            "learned_rms_px": rms(learned), "plain_sweep_rms_px": rms(plain), "pixels": int(m.sum())}
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -319,6 +339,19 @@ def run_ours(args):
             "value": round(ws * px / (ms_m * 1e-3) / 1e6, 3), "unit": "Mpx/s", "ms_per_step": round(ms_m, 4),
             "stage_ms": {"transform": round(st_m[0], 4), "search": round(st_m[1], 4),
                          "agree_subpixel": round(st_m[2], 4)}}
+
+    if not args.no_learned and N.load().bicos_learned_model_installed():
+        # the learned subpixel form (extension): network proposal, one
+        # reference NCC check, the reference sweep where the check fails
+        ms_l, st_l, out_l = timed(False, args.steps, 2, stage_times=True, form=2)
+        result["learned_form"] = {
+            "value": round(ws * px / (ms_l * 1e-3) / 1e6, 3), "unit": "Mpx/s", "ms_per_step": round(ms_l, 4),
+            "vs_plain_sweep": round(ms / ms_l, 3),
+            "stage_ms": {"transform": round(st_l[0], 4), "search": round(st_l[1], 4),
+                         "agree_learned": round(st_l[2], 4)},
+            "agree_stage_vs_plain_sweep": round(stages[2] / st_l[2], 3),
+            "gpu_launches_per_step": 6,
+            "error": learned_error(lbg, pybicos, left, right, out[0], out_l[0], n)}
 
     if not args.no_e2e:
         # host path: pinned host stacks -> bicos_match_host_v1 (upload, match, download)

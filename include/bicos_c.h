@@ -91,7 +91,8 @@ typedef struct bicos_config {
     int32_t no_dupes;         /* Consistency only, default 0 */
     int32_t max_bits;         /* descriptor width limit: 256 as the reference;
                                  up to 512 accepts FULL stacks of n <= 23 (extension) */
-    int32_t nxcorr_form;      /* BICOS_NXCORR_REFERENCE (default) or BICOS_NXCORR_MOMENTS */
+    int32_t nxcorr_form;      /* BICOS_NXCORR_REFERENCE (default), BICOS_NXCORR_MOMENTS or
+                                 BICOS_NXCORR_LEARNED */
 } bicos_config;
 
 /* NCC forms.  REFERENCE: the reference's two-pass NCC, bit-identical
@@ -101,7 +102,16 @@ typedef struct bicos_config {
  * correlation is a closed-form function of the position; FP64 (precision
  * double) or FP32 evaluates only the final polynomials and ratio.  Results
  * differ from the reference's by the rounding of its interpolants. */
-enum { BICOS_NXCORR_REFERENCE = 0, BICOS_NXCORR_MOMENTS = 1 };
+enum { BICOS_NXCORR_REFERENCE = 0, BICOS_NXCORR_MOMENTS = 1, BICOS_NXCORR_LEARNED = 2 };
+/* LEARNED (extension, no counterpart in the reference; subpixel runs only,
+ * other runs take the reference form): a small network proposes each
+ * match's subpixel offset x from the correlations at the integer disparities
+ * d-2..d+2 and the per-pixel variances; one NCC evaluation in the
+ * reference's arithmetic (its rounded interpolants, its precision) at x
+ * accepts the proposal when rho(x) >= rho(d) - 0.002, giving d - x and
+ * rho(x) exactly as the sweep would for that x; every other pixel takes the
+ * reference sweep with the configured step.  Needs an installed model
+ * (bicos_learned_model_v1; the library carries a trained one). */
 
 /* Fills the reference defaults (include/common.hpp:73-82). */
 bicos_status bicos_config_default(bicos_config* cfg);
@@ -205,6 +215,47 @@ bicos_status bicos_agree_subpixel_v1(const bicos_image* raw_disparity, const bic
                                      int32_t has_min_var, float min_var, int32_t precision,
                                      bicos_image* disparity, bicos_image* corrmap,
                                      bicos_stream_t stream);
+
+/*
+ * Learned subpixel form (extension; no counterpart in the reference).
+ *
+ * bicos_subpixel_features_v1: per pixel of a raw int16 disparity, 8 floats
+ *   into `features` (float32, rows x 8*cols, 16-byte aligned rows): the
+ *   correlation of the left pixel with the right columns col1-2..col1+2
+ *   (NaN outside the image), the left and right per-frame variances, and 1
+ *   (0 and NaNs for invalid matches).  Exact integer moments, FP32 ratio.
+ * bicos_agree_learned_v1: the LEARNED agreement stage of a raw disparity,
+ *   arguments as bicos_agree_subpixel_v1 (min_var already scaled by n);
+ *   optionally the network's proposals (float32 image) and, after the
+ *   stream completes, the number of pixels that fell back to the sweep.
+ * bicos_learned_model_v1: installs a model file image ("BICOSMLP" version
+ *   1: header, FP32 input statistics, BF16 parameters) for this process,
+ *   replacing the built-in one; NULL uninstalls.  Not to be called while
+ *   matches in the learned form are in flight.
+ * bicos_mlp_*: the network's own training kernels on device buffers (model
+ *   layout: parameters, then 7 input means and 7 standard deviations;
+ *   samples: 8 floats, the feature row with the target offset in the last
+ *   slot): gradient sum and loss of a batch, an Adam step, and the
+ *   proposals of feature rows as the learned form computes them.
+ */
+bicos_status bicos_subpixel_features_v1(const bicos_image* raw_disparity, const bicos_image* stack0,
+                                        const bicos_image* stack1, uint32_t n, bicos_image* features,
+                                        bicos_stream_t stream);
+bicos_status bicos_agree_learned_v1(const bicos_image* raw_disparity, const bicos_image* stack0,
+                                    const bicos_image* stack1, uint32_t n, float nxcorr_threshold,
+                                    float subpixel_step, int32_t has_min_var, float min_var, int32_t precision,
+                                    bicos_image* disparity, bicos_image* corrmap, bicos_image* proposals,
+                                    int32_t* fallback_count, bicos_stream_t stream);
+bicos_status bicos_learned_model_v1(const void* data, size_t nbytes);
+int bicos_learned_model_installed(void);
+bicos_status bicos_learned_model_floats_v1(float* out, int capacity);
+void bicos_mlp_sizes(int* n_params, int* n_model_floats);
+bicos_status bicos_mlp_grad_v1(const float* model, const float* samples, int count, float* grad, float* loss,
+                               void* stream);
+bicos_status bicos_mlp_adam_v1(float* params, float* grad, float* m, float* v, int step, float lr,
+                               float scale, void* stream);
+bicos_status bicos_mlp_propose_v1(const float* model, const float* features, int count, float* out,
+                                  void* stream);
 
 /*
  * Stage timing for measurement tools (no counterpart in the reference,

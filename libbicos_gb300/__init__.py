@@ -19,6 +19,7 @@ from .pybicos import Config, Precision, TransformMode, Variant
 
 __all__ = ["pybicos", "Config", "Precision", "TransformMode", "Variant", "match_device",
            "descriptor_transform", "search", "agree", "agree_subpixel", "descriptor_words",
+           "subpixel_features", "agree_learned",
            "load_library", "required_bits"]
 
 
@@ -144,3 +145,37 @@ def agree_subpixel(raw, stack0, stack1, threshold: float, step: float, min_var=N
                                             float(min_var or 0.0), int(double), C.byref(oi), C.byref(ci),
                                             _stream_ptr(stream)))
     return out, corr
+
+
+def subpixel_features(raw, stack0, stack1, stream=None):
+    """Feature rows of the learned subpixel form for an int16 raw disparity:
+    (rows, cols, 8) float32 -- rho at col1-2..col1+2, left and right
+    per-frame variances, validity flag."""
+    import torch
+    a0, n, f0 = _frames(stack0)
+    a1, _, _ = _frames(stack1)
+    rows, cols = raw.shape
+    feats = torch.empty((rows, cols, 8), dtype=torch.float32, device=raw.device)
+    ri = N.tensor_image(raw)
+    fi = N.image(feats.data_ptr(), rows, 8 * cols, N.BICOS_32F, 32 * cols)
+    _raise(N.load().bicos_subpixel_features_v1(C.byref(ri), a0, a1, n, C.byref(fi), _stream_ptr(stream)))
+    return feats
+
+
+def agree_learned(raw, stack0, stack1, threshold: float, step: float, min_var=None, double=False, stream=None):
+    """Learned-form agreement of an int16 raw disparity: returns (float32
+    disparity, corrmap, proposals, number of pixels that took the sweep).
+    min_var is the per-stack value (min_variance * n)."""
+    import torch
+    a0, n, f0 = _frames(stack0)
+    a1, _, _ = _frames(stack1)
+    out = torch.empty(raw.shape, dtype=torch.float32, device=raw.device)
+    corr = torch.empty(raw.shape, dtype=torch.float64 if double else torch.float32, device=raw.device)
+    prop = torch.empty(raw.shape, dtype=torch.float32, device=raw.device)
+    ri, oi, ci, pi = N.tensor_image(raw), N.tensor_image(out), N.tensor_image(corr), N.tensor_image(prop)
+    count = C.c_int32(-1)
+    _raise(N.load().bicos_agree_learned_v1(C.byref(ri), a0, a1, n, threshold, step, int(min_var is not None),
+                                           float(min_var or 0.0), int(double), C.byref(oi), C.byref(ci),
+                                           C.byref(pi), C.byref(count), _stream_ptr(stream)))
+    (torch.cuda.current_stream(raw.device) if stream is None else stream).synchronize()  # the count is host memory
+    return out, corr, prop, int(count.value)

@@ -12,6 +12,7 @@ from . import build as _build
 
 BICOS_8U, BICOS_16U, BICOS_16S, BICOS_32F, BICOS_64F = 0, 2, 3, 5, 6
 OK, ERR_EXCEPTION, ERR_INVALID_ARGUMENT, ERR_CUDA = 0, 1, 2, 3
+NXCORR_REFERENCE, NXCORR_MOMENTS, NXCORR_LEARNED = 0, 1, 2
 FLAG_NODUPES, FLAG_CONSISTENCY = 1, 2
 
 _TYPE_OF_DTYPE = {"uint8": BICOS_8U, "uint16": BICOS_16U, "int16": BICOS_16S,
@@ -78,6 +79,15 @@ def load():
         "bicos_search_noalloc_v1": ([P, P, I, I, U, I, I, IMG, P], C.c_int),
         "bicos_agree_v1": ([IMG, IMG, IMG, U, F, I, F, I, IMG, P], C.c_int),
         "bicos_agree_subpixel_v1": ([IMG, IMG, IMG, U, F, F, I, F, I, IMG, IMG, P], C.c_int),
+        "bicos_subpixel_features_v1": ([IMG, IMG, IMG, U, IMG, P], C.c_int),
+        "bicos_agree_learned_v1": ([IMG, IMG, IMG, U, F, F, I, F, I, IMG, IMG, IMG, C.POINTER(I), P], C.c_int),
+        "bicos_learned_model_v1": ([P, S], C.c_int),
+        "bicos_learned_model_installed": ([], C.c_int),
+        "bicos_learned_model_floats_v1": ([P, C.c_int], C.c_int),
+        "bicos_mlp_sizes": ([C.POINTER(C.c_int), C.POINTER(C.c_int)], None),
+        "bicos_mlp_grad_v1": ([P, P, C.c_int, P, P, P], C.c_int),
+        "bicos_mlp_adam_v1": ([P, P, P, P, C.c_int, F, F, P], C.c_int),
+        "bicos_mlp_propose_v1": ([P, P, C.c_int, P, P], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

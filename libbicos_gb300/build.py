@@ -19,6 +19,9 @@ CSRC = os.path.join(PKG, "csrc")
 OUT_DIR = os.path.join(PKG, "_lib")
 OBJ_DIR = os.path.join(OUT_DIR, "obj")
 LIB = os.path.join(OUT_DIR, "libbicos_gb300.so")
+GEN_DIR = os.path.join(OUT_DIR, "gen")
+# trained weights of the learned subpixel proposal, compiled into the library
+MODEL = os.path.join(PKG, "learned_subpixel.bsm")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",
@@ -34,6 +37,24 @@ def nvcc() -> str:
 
 def sources() -> list[str]:
     return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cpp")))
+
+
+def model_blob() -> str:
+    """C++ source holding the model file's bytes (empty when there is no
+    model file); rewritten only when its content changes."""
+    data = open(MODEL, "rb").read() if os.path.exists(MODEL) else b""
+    body = ",".join(str(b) for b in data) or "0"
+    text = ("// generated by libbicos_gb300/build.py from learned_subpixel.bsm\n"
+            "namespace bicos_gb300 {\n"
+            f"extern const unsigned char kEmbeddedModel[] = {{{body}}};\n"
+            f"extern const unsigned long long kEmbeddedModelSize = {len(data)}ull;\n"
+            "}\n")
+    os.makedirs(GEN_DIR, exist_ok=True)
+    path = os.path.join(GEN_DIR, "learned_model_blob.cpp")
+    if not os.path.exists(path) or open(path).read() != text:
+        with open(path, "w") as f:
+            f.write(text)
+    return path
 
 
 def _deps_newer(obj: str, src: str) -> bool:
@@ -61,7 +82,7 @@ def _compile(src: str, extra: list[str]) -> str:
 
 def build(verbose: bool = False, extra: list[str] | None = None) -> str:
     os.makedirs(OBJ_DIR, exist_ok=True)
-    srcs = sources()
+    srcs = sources() + [model_blob()]
     with cf.ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(lambda s: _compile(s, extra or []), srcs))
     if not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):

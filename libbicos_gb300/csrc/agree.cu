@@ -17,15 +17,10 @@
 #include <type_traits>
 
 #include "kernels.cuh"
+#include "ncc.cuh"
 
 namespace bicos_gb300 {
 namespace {
-
-template<typename T>
-__device__ __forceinline__ int ld_px(const StackParams& p, int side, int t, int row, int col) {
-    const T* r = reinterpret_cast<const T*>(p.frame[side][t] + (long long)row * p.pitch[side][t]);
-    return (int)__ldg(r + col);
-}
 
 template<typename TP>
 __device__ __forceinline__ void put_corr(const AgreeParams& p, int row, int col, TP v) {
@@ -113,17 +108,6 @@ __device__ __forceinline__ void left_d(const int (&x)[NMAX], int n, double (&d0)
         }
 }
 
-template<bool DBL>
-struct Prec;
-template<>
-struct Prec<false> {
-    using T = float;
-};
-template<>
-struct Prec<true> {
-    using T = double;
-};
-
 template<bool DBL, int NMAX>
 __device__ __forceinline__ typename Prec<DBL>::T nxc_full(const int (&x)[NMAX], const int (&y)[NMAX], int n,
                                                           bool mv, float minvar) {
@@ -171,21 +155,45 @@ __global__ void __launch_bounds__(128) k_agree(const __grid_constant__ AgreePara
         *dp = kInvalidDisp;
 }
 
-// (T)__float2int_rn(v): round half to even, wrap modulo 2^bits
-template<typename T>
-__device__ __forceinline__ int round_wrap(float v) {
-    return (int)(T)__float2int_rn(v);
+// per-frame coefficients of the quadratic through the right columns
+// col1-1, col1, col1+1 (agree.hpp:120-140): a = (y0 - 2 y1 + y2) / 2,
+// b = (y2 - y0) / 2, c = y1, all exact in float
+template<typename T, int NMAX>
+__device__ __forceinline__ void interp_coef(const StackParams& s, int row, int col1, float (&a)[NMAX],
+                                            float (&b)[NMAX], float (&c)[NMAX]) {
+#pragma unroll
+    for (int t = 0; t < NMAX; ++t) {
+        if (t < s.n) {
+            const int y0 = ld_px<T>(s, 1, t, row, col1 - 1);
+            const int y1 = ld_px<T>(s, 1, t, row, col1);
+            const int y2 = ld_px<T>(s, 1, t, row, col1 + 1);
+            a[t] = 0.5f * (float)(y0 - 2 * y1 + y2);
+            b[t] = 0.5f * (float)(y2 - y0);
+            c[t] = (float)y1;
+        } else {
+            a[t] = b[t] = c[t] = 0.f;
+        }
+    }
 }
 
-// agree_subpixel (agree.hpp:94-185, agree.cuh:161-259)
+// the interpolants at x as the input type: ((a*x)*x + b*x) + c, each step
+// rounded, then round half to even and wrap
+template<typename T, int NMAX>
+__device__ __forceinline__ void interp_at(const float (&a)[NMAX], const float (&b)[NMAX], const float (&c)[NMAX],
+                                          int n, float x, int (&iv)[NMAX]) {
+#pragma unroll
+    for (int t = 0; t < NMAX; ++t) {
+        const float q = __fadd_rn(__fadd_rn(__fmul_rn(__fmul_rn(a[t], x), x), __fmul_rn(b[t], x)), c[t]);
+        iv[t] = t < n ? round_wrap<T>(q) : 0;
+    }
+}
+
+// agree_subpixel of one pixel (agree.hpp:94-185, agree.cuh:161-259),
+// writing its disparity and correlation
 template<typename T, bool DBL, int NMAX>
-__global__ void __launch_bounds__(128) k_agree_subpixel(const __grid_constant__ AgreeParams p) {
+__device__ void sweep_pixel(const AgreeParams& p, int row, int col) {
     using TP = typename Prec<DBL>::T;
-    const int col = blockIdx.x * blockDim.x + threadIdx.x;
-    const int row = blockIdx.y;
     const int cols = p.s.cols, n = p.s.n;
-    if (col >= cols)
-        return;
     float result = NAN;
     TP corr = (TP)NAN;
     const int16_t d = reinterpret_cast<const int16_t*>(reinterpret_cast<const char*>(p.raw) + row * p.raw_pitch)[col];
@@ -207,20 +215,7 @@ __global__ void __launch_bounds__(128) k_agree_subpixel(const __grid_constant__ 
                 result = (float)d;
         } else {
             float a[NMAX], b[NMAX], c[NMAX];
-#pragma unroll
-            for (int t = 0; t < NMAX; ++t) {
-                if (t < n) {
-                    const int y0 = ld_px<T>(p.s, 1, t, row, col1 - 1);
-                    const int y1 = ld_px<T>(p.s, 1, t, row, col1);
-                    const int y2 = ld_px<T>(p.s, 1, t, row, col1 + 1);
-                    // 0.5f*(y0 - 2y1 + y2), 0.5f*(-y0 + y2), y1: exact in float
-                    a[t] = 0.5f * (float)(y0 - 2 * y1 + y2);
-                    b[t] = 0.5f * (float)(y2 - y0);
-                    c[t] = (float)y1;
-                } else {
-                    a[t] = b[t] = c[t] = 0.f;
-                }
-            }
+            interp_coef<T>(p.s, row, col1, a, b, c);
             TP d0[NMAX], var0;
             if constexpr (DBL)
                 left_d(x, n, d0, var0);
@@ -231,11 +226,7 @@ __global__ void __launch_bounds__(128) k_agree_subpixel(const __grid_constant__ 
             TP best = (TP)-1.0;
             for (float xs = -1.f; xs <= 1.f; xs = __fadd_rn(xs, p.step)) {
                 int iv[NMAX];
-#pragma unroll
-                for (int t = 0; t < NMAX; ++t) {
-                    const float q = __fadd_rn(__fadd_rn(__fmul_rn(__fmul_rn(a[t], xs), xs), __fmul_rn(b[t], xs)), c[t]);
-                    iv[t] = t < n ? round_wrap<T>(q) : 0;
-                }
+                interp_at<T>(a, b, c, n, xs, iv);
                 TP nxc;
                 if constexpr (DBL)
                     nxc = nxc_d(d0, var0, iv, n, mv, (double)p.minvar);
@@ -255,8 +246,20 @@ __global__ void __launch_bounds__(128) k_agree_subpixel(const __grid_constant__ 
     put_corr<TP>(p, row, col, corr);
 }
 
-// Single-precision subpixel sweep, same results as k_agree_subpixel<T,
-// false, NMAX>, organised for throughput:
+// the sweep over the pixels of a list (the learned form's fallback);
+// grid-stride over a length that only the device knows
+template<typename T, bool DBL, int NMAX>
+__global__ void __launch_bounds__(128) k_subpixel_list(const __grid_constant__ AgreeParams p,
+                                                       const int* __restrict__ list, const int* __restrict__ count) {
+    const int total = *count;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const int px = list[i];
+        sweep_pixel<T, DBL, NMAX>(p, px / p.s.cols, px % p.s.cols);
+    }
+}
+
+// Single-precision subpixel sweep, same results as sweep_pixel<T, false,
+// NMAX> over every pixel, organised for throughput:
 //  - per pixel, the frame coefficients (a, b, c) and the centred left
 //    samples d0 are staged once in shared memory as one float4 per frame
 //    (each thread reads back only its own column, so no barrier is needed);
@@ -401,7 +404,7 @@ __global__ void __launch_bounds__(kSubThreads) k_subpixel_f32(const __grid_const
     put_corr<float>(p, row, col, corr);
 }
 
-// Double-precision subpixel sweep, same results as k_agree_subpixel<T,
+// Double-precision subpixel sweep, same results as sweep_pixel<T,
 // true, NMAX> (the reference's nxcorrd, include/impl/cuda/agree.cuh:35-65),
 // with FP64 work only where it can decide the result:
 //  - one pass over the sweep forms, per point, the exact integer moments
@@ -660,7 +663,39 @@ cudaError_t launch_any(const AgreeParams& p, bool dbl, cudaStream_t st) {
     return dbl ? launch_t<uint16_t, true, SUB>(p, st) : launch_t<uint16_t, false, SUB>(p, st);
 }
 
+template<typename T, bool DBL>
+cudaError_t launch_list_t(const AgreeParams& p, const int* list, const int* count, cudaStream_t st) {
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess)
+        e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess)
+        return e;
+    const int blocks = sms * 8;  // grid-stride; the list length is known on the device only
+    const int n = p.s.n;
+#define BICOS_LIST_CASE(NM)                                                    \
+    if (n <= NM) {                                                             \
+        k_subpixel_list<T, DBL, NM><<<blocks, 128, 0, st>>>(p, list, count); \
+        return cudaGetLastError();                                             \
+    }
+    BICOS_LIST_CASE(8)
+    BICOS_LIST_CASE(16)
+    BICOS_LIST_CASE(24)
+    BICOS_LIST_CASE(33)
+    BICOS_LIST_CASE(48)
+    BICOS_LIST_CASE(65)
+#undef BICOS_LIST_CASE
+    return cudaErrorInvalidValue;
+}
+
 }  // namespace
+
+cudaError_t launch_subpixel_list(const AgreeParams& p, bool dbl, const int* list, const int* count,
+                                 cudaStream_t st) {
+    if (p.s.elem_bytes == 1)
+        return dbl ? launch_list_t<uint8_t, true>(p, list, count, st) : launch_list_t<uint8_t, false>(p, list, count, st);
+    return dbl ? launch_list_t<uint16_t, true>(p, list, count, st) : launch_list_t<uint16_t, false>(p, list, count, st);
+}
 
 cudaError_t launch_agree(const AgreeParams& p, bool dbl, cudaStream_t st) {
     return launch_any<false>(p, dbl, st);

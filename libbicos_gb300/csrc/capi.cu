@@ -197,6 +197,44 @@ struct DeviceGuard {
     DeviceGuard() { err = cudaGetDevice(&dev); }
 };
 
+// the learned form accepts a proposal when rho(x) >= rho(0) - kLearnedDrop
+constexpr float kLearnedDrop = 0.002f;
+
+// scratch of the learned form: the fallback list (one int per pixel) and
+// its length
+size_t learned_scratch_bytes(size_t px) { return align_up(px * 4, 256) + 256; }
+
+// Learned subpixel stage: one fused pass (features -> network -> one
+// reference NCC check per pixel), then the reference sweep over the pixels
+// whose check failed.  `ap` carries the raw disparity, the float output and
+// the corrmap; `scratch` holds learned_scratch_bytes(px).
+cudaError_t learned_subpixel(const AgreeParams& ap, bool dbl, const float* model, void* scratch,
+                             int* fallback_count_out, float* proposal, long long proposal_pitch,
+                             cudaStream_t st) {
+    const size_t px = (size_t)ap.s.rows * ap.s.cols;
+    char* b = static_cast<char*>(scratch);
+    int* list = reinterpret_cast<int*>(b);
+    int* count = reinterpret_cast<int*>(b + align_up(px * 4, 256));
+    cudaError_t e = cudaMemsetAsync(count, 0, sizeof(int), st);
+    if (e == cudaSuccess) {
+        LearnedParams lp;
+        std::memset(&lp, 0, sizeof lp);
+        lp.a = ap;
+        lp.model = model;
+        lp.proposal = proposal;
+        lp.proposal_pitch = proposal_pitch;
+        lp.list = list;
+        lp.count = count;
+        lp.drop = kLearnedDrop;
+        e = launch_learned(lp, dbl, st);
+    }
+    if (e == cudaSuccess)
+        e = launch_subpixel_list(ap, dbl, list, count, st);
+    if (e == cudaSuccess && fallback_count_out)
+        e = cudaMemcpyAsync(fallback_count_out, count, sizeof(int), cudaMemcpyDeviceToHost, st);
+    return e;
+}
+
 }  // namespace
 
 void bicos_gb300::set_last_error(const std::string& msg) { g_last_error = msg; }
@@ -238,7 +276,9 @@ int32_t bicos_descriptor_words(uint32_t n, int32_t mode, int32_t max_bits) {
     return words_for((int)n, mode == BICOS_MODE_FULL, max_bits);
 }
 
-int32_t bicos_kernel_faults(void) { return (int32_t)(read_tc_faults() + read_moment_faults()); }
+int32_t bicos_kernel_faults(void) {
+    return (int32_t)(read_tc_faults() + read_moment_faults() + read_mlp_faults());
+}
 
 bicos_status bicos_stage_timing(int32_t enable) {
     std::lock_guard<std::mutex> lk(g_timing.mu);
@@ -306,6 +346,8 @@ bicos_status bicos_match_v1(const bicos_image* stack0, const bicos_image* stack1
     if (sub && !step_ok(cfg->subpixel_step))
         return fail(BICOS_ERR_EXCEPTION, "subpixel step must be a finite value >= 1e-4");
     const bool consistency = cfg->variant == BICOS_VARIANT_CONSISTENCY;
+    if (cfg->nxcorr_form < BICOS_NXCORR_REFERENCE || cfg->nxcorr_form > BICOS_NXCORR_LEARNED)
+        return fail(BICOS_ERR_INVALID_ARGUMENT, "unknown nxcorr_form " + std::to_string(cfg->nxcorr_form));
     if (!image_ok(disparity, rows, cols, sub ? BICOS_32F : BICOS_16S))
         return fail(BICOS_ERR_EXCEPTION, sub ? "disparity must be a float32 image of the stack's size"
                                              : "disparity must be an int16 image of the stack's size");
@@ -317,13 +359,23 @@ bicos_status bicos_match_v1(const bicos_image* stack0, const bicos_image* stack1
     if (g.err != cudaSuccess)
         return cuda_fail(g.err, "cudaGetDevice");
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const bool learned = sub && cfg->nxcorr_form == BICOS_NXCORR_LEARNED;
+    const float* model = nullptr;
+    if (learned) {
+        std::string err;
+        model = learned_model_device(st, &err);
+        if (!model)
+            return fail(BICOS_ERR_INVALID_ARGUMENT, err);
+    }
 
-    // scratch: descriptors of both sides, raw disparity, consistency bests
+    // scratch: descriptors of both sides, raw disparity, consistency bests,
+    // the learned form's buffers
     const size_t px = (size_t)rows * cols;
     const size_t desc_bytes = align_up(px * nw * 4, 256);
     const size_t raw_bytes = sub ? align_up(px * 2, 256) : 0;
     const size_t best_bytes = consistency ? align_up(px * 4, 256) : 0;
-    const size_t need = 2 * desc_bytes + raw_bytes + 2 * best_bytes;
+    const size_t learned_bytes = learned ? learned_scratch_bytes(px) : 0;
+    const size_t need = 2 * desc_bytes + raw_bytes + 2 * best_bytes + learned_bytes;
 
     Scratch& s = g_scratch[g.dev % kMaxDevices];
     std::lock_guard<std::mutex> lk(s.mu);
@@ -380,6 +432,14 @@ bicos_status bicos_match_v1(const bicos_image* stack0, const bicos_image* stack1
             mp.has_minvar = ap.has_minvar;
             mp.minvar = ap.minvar;
             e = launch_moments(mp, sub ? 1 : 0, dbl, st);
+        } else if (learned) {
+            ap.raw = raw;
+            ap.raw_pitch = raw_pitch;
+            ap.out = disparity->data;
+            ap.out_pitch = (long long)disparity->step;
+            ap.step = cfg->subpixel_step;
+            e = learned_subpixel(ap, dbl, model, b + 2 * desc_bytes + raw_bytes + 2 * best_bytes, nullptr, nullptr,
+                                 0, st);
         } else if (sub) {
             ap.raw = raw;
             ap.raw_pitch = raw_pitch;
@@ -598,6 +658,92 @@ bicos_status bicos_agree_subpixel_v1(const bicos_image* raw_disparity, const bic
     cudaError_t e = launch_agree_subpixel(ap, dbl, reinterpret_cast<cudaStream_t>(stream));
     if (e != cudaSuccess)
         return cuda_fail(e, "agree_subpixel launch");
+    return BICOS_OK;
+}
+
+bicos_status bicos_subpixel_features_v1(const bicos_image* raw_disparity, const bicos_image* stack0,
+                                        const bicos_image* stack1, uint32_t n, bicos_image* features,
+                                        bicos_stream_t stream) {
+    int eb = 0;
+    if (bicos_status s = check_stacks(stack0, stack1, n, &eb))
+        return s;
+    if (n > (uint32_t)kMaxFrames)
+        return fail(BICOS_ERR_EXCEPTION, "Bad number of images");
+    const int rows = stack0[0].rows, cols = stack0[0].cols;
+    if (!image_ok(raw_disparity, rows, cols, BICOS_16S))
+        return fail(BICOS_ERR_EXCEPTION, "raw disparity must be an int16 image of the stack's size");
+    if (!features || !features->data || features->rows != rows || features->cols != 8 * cols ||
+        features->type != BICOS_32F || features->step < (size_t)cols * 32 || features->step % 16 != 0 ||
+        reinterpret_cast<uintptr_t>(features->data) % 16 != 0)
+        return fail(BICOS_ERR_EXCEPTION, "features must be a 16-byte aligned float32 image of rows x 8*cols");
+    MomentParams mp;
+    std::memset(&mp, 0, sizeof mp);
+    fill_stack(mp.s, stack0, stack1, n, eb);
+    mp.raw = static_cast<const int16_t*>(raw_disparity->data);
+    mp.raw_pitch = (long long)raw_disparity->step;
+    mp.out = features->data;
+    mp.out_pitch = (long long)features->step;
+    cudaError_t e = launch_moments(mp, 2, false, reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess)
+        return cuda_fail(e, "features launch");
+    return BICOS_OK;
+}
+
+bicos_status bicos_agree_learned_v1(const bicos_image* raw_disparity, const bicos_image* stack0,
+                                    const bicos_image* stack1, uint32_t n, float nxcorr_threshold,
+                                    float subpixel_step, int32_t has_min_var, float min_var, int32_t precision,
+                                    bicos_image* disparity, bicos_image* corrmap, bicos_image* proposals,
+                                    int32_t* fallback_count, bicos_stream_t stream) {
+    int eb = 0;
+    if (bicos_status s = check_stacks(stack0, stack1, n, &eb))
+        return s;
+    if (n > (uint32_t)kMaxFrames)
+        return fail(BICOS_ERR_EXCEPTION, "Bad number of images");
+    const int rows = stack0[0].rows, cols = stack0[0].cols;
+    const bool dbl = precision == BICOS_PRECISION_DOUBLE;
+    if (!step_ok(subpixel_step))
+        return fail(BICOS_ERR_EXCEPTION, "subpixel step must be a finite value >= 1e-4");
+    if (!image_ok(raw_disparity, rows, cols, BICOS_16S))
+        return fail(BICOS_ERR_EXCEPTION, "raw disparity must be an int16 image of the stack's size");
+    if (!image_ok(disparity, rows, cols, BICOS_32F))
+        return fail(BICOS_ERR_EXCEPTION, "disparity must be a float32 image of the stack's size");
+    if (corrmap && !image_ok(corrmap, rows, cols, dbl ? BICOS_64F : BICOS_32F))
+        return fail(BICOS_ERR_EXCEPTION, "corrmap type or size mismatch");
+    if (proposals && !image_ok(proposals, rows, cols, BICOS_32F))
+        return fail(BICOS_ERR_EXCEPTION, "proposals must be a float32 image of the stack's size");
+    DeviceGuard g;
+    if (g.err != cudaSuccess)
+        return cuda_fail(g.err, "cudaGetDevice");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    std::string err;
+    const float* model = learned_model_device(st, &err);
+    if (!model)
+        return fail(BICOS_ERR_INVALID_ARGUMENT, err);
+    AgreeParams ap;
+    std::memset(&ap, 0, sizeof ap);
+    fill_stack(ap.s, stack0, stack1, n, eb);
+    ap.raw = static_cast<const int16_t*>(raw_disparity->data);
+    ap.raw_pitch = (long long)raw_disparity->step;
+    ap.out = disparity->data;
+    ap.out_pitch = (long long)disparity->step;
+    ap.thr = nxcorr_threshold;
+    ap.step = subpixel_step;
+    ap.has_minvar = has_min_var != 0;
+    ap.minvar = min_var;
+    ap.corr = corrmap ? corrmap->data : nullptr;
+    ap.corr_pitch = corrmap ? (long long)corrmap->step : 0;
+    Scratch& s = g_scratch[g.dev % kMaxDevices];
+    std::lock_guard<std::mutex> lk(s.mu);
+    void* base = nullptr;
+    BICOS_CUDA_TRY(scratch_acquire(s, learned_scratch_bytes((size_t)rows * cols), st, &base));
+    cudaError_t e = learned_subpixel(ap, dbl, model, base, fallback_count,
+                                     proposals ? static_cast<float*>(proposals->data) : nullptr,
+                                     proposals ? (long long)proposals->step : 0, st);
+    cudaError_t er = scratch_release(s, st);
+    if (e == cudaSuccess)
+        e = er;
+    if (e != cudaSuccess)
+        return cuda_fail(e, "learned agree launch");
     return BICOS_OK;
 }
 

@@ -85,6 +85,39 @@ cudaError_t launch_consistency(const int32_t* fwd, const int32_t* rev, int rows,
 cudaError_t launch_agree(const AgreeParams& p, bool dbl, cudaStream_t st);
 cudaError_t launch_agree_subpixel(const AgreeParams& p, bool dbl, cudaStream_t st);
 
+// learned subpixel form (learned.cu): per pixel features -> network
+// proposal -> one reference NCC check; pixels whose check fails are
+// appended to `list` for the reference sweep (launch_subpixel_list)
+struct LearnedParams {
+    AgreeParams a;             // raw in, float disparity out, corrmap, threshold, min_var
+    const float* model;        // device model buffer (mlp_model_floats() floats)
+    float* proposal;           // optional per-pixel offsets (NaN where no proposal), may be null
+    long long proposal_pitch;
+    int* list;                 // pixels (row * cols + col) left to the sweep
+    int* count;                // length of list, zeroed before the launch
+    float drop;                // accepted when rho(x) >= rho(0) - drop
+};
+cudaError_t launch_learned(const LearnedParams& p, bool dbl, cudaStream_t st);
+// the reference sweep over the pixels of a list (agree.cu)
+cudaError_t launch_subpixel_list(const AgreeParams& p, bool dbl, const int* list, const int* count,
+                                 cudaStream_t st);
+
+// subpixel network (learned.cu); a model buffer holds mlp_model_floats()
+// floats: the parameters, then the input means and standard deviations
+int mlp_param_count();
+int mlp_model_floats();
+cudaError_t launch_mlp_grad(const float* model, const float* samples, int count, float* grad, float* loss,
+                            cudaStream_t st);
+cudaError_t launch_mlp_adam(float* params, float* grad, float* m, float* v, int step, float lr, float scale,
+                            cudaStream_t st);
+// proposals for `count` feature rows of 8 floats (BF16 weights, tensor cores)
+cudaError_t launch_mlp_propose(const float* model, const float* features, int count, float* out,
+                               cudaStream_t st);
+unsigned int read_mlp_faults();
+// device copy of the installed model for the current device (nullptr and a
+// message when none is installed)
+const float* learned_model_device(cudaStream_t st, std::string* err);
+
 // sets the per-thread message bicos_last_error() returns (defined in capi.cu)
 void set_last_error(const std::string& msg);
 

@@ -103,7 +103,9 @@ class Config:
         self.precision = Precision.Single
         self.variant = Variant.NoDuplicates()
         # extension (not in the reference): 0 = the reference's two-pass NCC,
-        # 1 = the moment form (tensor-core Sxy, unrounded subpixel interpolant)
+        # 1 = the moment form (tensor-core Sxy, unrounded subpixel interpolant),
+        # 2 = the learned subpixel form (network proposal, one reference NCC
+        # check, the reference sweep where the check fails)
         self.nxcorr_form = 0
 
     nxcorr_threshold = property(lambda s: s._thr, lambda s, v: setattr(s, "_thr", _f32(v)))
@@ -127,8 +129,8 @@ class Config:
             raise TypeError("mode must be a TransformMode and precision a Precision")
         c.mode = self.mode.value
         c.precision = self.precision.value
-        if self.nxcorr_form not in (0, 1):
-            raise ValueError("nxcorr_form must be 0 (reference) or 1 (moments)")
+        if self.nxcorr_form not in (0, 1, 2):
+            raise ValueError("nxcorr_form must be 0 (reference), 1 (moments) or 2 (learned)")
         c.nxcorr_form = int(self.nxcorr_form)
         if isinstance(self.variant, _Consistency):
             c.variant = 1

@@ -290,6 +290,11 @@ typedef struct {
     int dbl;
     float* out;
     void* corr;
+    /* learned-form check */
+    const float* proposal;
+    const float* features;
+    float drop;
+    uint8_t* fallback;
 } agree_ctx;
 
 static inline void put_corr(agree_ctx* c, size_t px, double v) {
@@ -463,6 +468,89 @@ void orc_agree_subpixel(const int16_t* disp, const void* s0, const void* s1, int
     parallel_rows(rows, nthreads, subpixel_rows, &c);
 }
 
+/* Learned form's check (the library's extension; restates agree.cu's
+ * k_learned_check): border pixels as the sweep; elsewhere one reference NCC
+ * at the proposed offset, accepted when rho(x) >= rho(0) - drop with rho(0)
+ * the feature row's integer-disparity correlation; rejected pixels are
+ * flagged for the sweep and left unwritten. */
+static void learned_rows(void* p, int r0, int r1) {
+    agree_ctx* c = (agree_ctx*)p;
+    const size_t plane = (size_t)c->rows * c->cols;
+    const int n = c->n;
+    int x[130], y[130], interp[130];
+    for (int r = r0; r < r1; ++r)
+        for (int col = 0; col < c->cols; ++col) {
+            const size_t px = (size_t)r * c->cols + col;
+            c->fallback[px] = 0;
+            const int16_t d = c->disp[px];
+            if (d == INVALID_I16)
+                continue;
+            const int col1 = col - d;
+            if (col1 < 0 || c->cols <= col1)
+                continue;
+            for (int t = 0; t < n; ++t)
+                x[t] = load_px(c->s0, c->elem_bytes, t * plane + px);
+            const size_t row1 = (size_t)r * c->cols;
+            if (col1 == 0 || col1 == c->cols - 1) {
+                for (int t = 0; t < n; ++t)
+                    y[t] = load_px(c->s1, c->elem_bytes, t * plane + row1 + col1);
+                const double nxc = nxc_px(c, x, y);
+                put_corr(c, px, nxc);
+                if (!below(c, nxc))
+                    c->out[px] = (float)d;
+                continue;
+            }
+            const float xo = c->proposal[px];
+            for (int t = 0; t < n; ++t) {
+                const int y0 = load_px(c->s1, c->elem_bytes, t * plane + row1 + col1 - 1);
+                const int y1 = load_px(c->s1, c->elem_bytes, t * plane + row1 + col1);
+                const int y2 = load_px(c->s1, c->elem_bytes, t * plane + row1 + col1 + 1);
+                const float a = 0.5f * ((float)y0 - 2.0f * (float)y1 + (float)y2);
+                const float b = 0.5f * (float)(-y0 + y2);
+                interp[t] = round_wrap(a * xo * xo + b * xo + (float)y1, c->elem_bytes);
+            }
+            const double nxc = nxc_px(c, x, interp);
+            const float r0f = c->features[8 * px + 2];
+            const double floor_rho = c->dbl ? (double)r0f - (double)c->drop : (double)(r0f - c->drop);
+            if (!(nxc >= floor_rho)) {
+                c->fallback[px] = 1;
+                continue;
+            }
+            put_corr(c, px, nxc);
+            if (!below(c, nxc))
+                c->out[px] = (float)d - xo;
+        }
+}
+
+void orc_learned_check(const int16_t* disp, const void* s0, const void* s1, int elem_bytes, int n, int rows,
+                       int cols, float thr, int has_minvar, float minvar, int dbl, const float* proposal,
+                       const float* features, float drop, float* out, void* corrmap, uint8_t* fallback,
+                       int nthreads) {
+    const size_t px = (size_t)rows * cols;
+    for (size_t i = 0; i < px; ++i)
+        out[i] = NAN;
+    agree_ctx c;
+    memset(&c, 0, sizeof c);
+    c.disp = disp;
+    c.s0 = s0;
+    c.s1 = s1;
+    c.elem_bytes = elem_bytes;
+    c.n = n;
+    c.rows = rows;
+    c.cols = cols;
+    c.thr = thr;
+    c.has_minvar = has_minvar;
+    c.minvar = minvar;
+    c.dbl = dbl;
+    c.out = out;
+    c.corr = corrmap;
+    c.proposal = proposal;
+    c.features = features;
+    c.drop = drop;
+    c.fallback = fallback;
+    parallel_rows(rows, nthreads, learned_rows, &c);
+}
+
 /* ---- dispatch, src/impl/cpu.cpp:96-155 ---- */
 
 int orc_required_bits(int n, int full) {
@@ -611,6 +699,26 @@ static void moments_rows(void* p, int r0, int r1) {
                             syy[j][k] += y[j] * y[k];
                 }
                 const long long v0 = nn * sxx - sx * sx;
+                if (c->mode == 2) {
+                    /* learned-form features: rho at col1-2..col1+2 (FP32
+                     * ratio, NaN outside the image), variances, flag */
+                    float* f = (float*)c->out + 8 * px;
+                    for (int j = 0; j < 5; ++j) {
+                        const int cc = col1 + j - 2;
+                        if (cc >= 0 && cc < c->cols) {
+                            const long long v1 = nn * syy[j][j] - sy[j] * sy[j];
+                            f[j] = (float)mom_ratio(0, mom_cvt(0, nn * sxy[j] - sx * sy[j]), mom_cvt(0, v0),
+                                                    mom_cvt(0, v1));
+                        } else {
+                            f[j] = NAN;
+                        }
+                    }
+                    const float n2 = (float)c->n * (float)c->n;
+                    f[5] = (float)v0 / n2;
+                    f[6] = (float)(nn * syy[2][2] - sy[2] * sy[2]) / n2;
+                    f[7] = 1.f;
+                    continue;
+                }
                 const double mvn = c->dbl ? (double)c->minvar * (double)c->n
                                           : (double)((float)c->minvar * (float)c->n);
                 const double V0 = mom_cvt(c->dbl, v0);
@@ -664,6 +772,13 @@ static void moments_rows(void* p, int r0, int r1) {
                     if (pass)
                         fout = (float)d - best_x;
                 }
+            }
+            if (c->mode == 2) {
+                float* f = (float*)c->out + 8 * px;
+                for (int j = 0; j < 7; ++j)
+                    f[j] = NAN;
+                f[7] = 0.f;
+                continue;
             }
             if (c->mode == 0)
                 ((int16_t*)c->out)[px] = iout;

@@ -79,10 +79,20 @@ double orc_nxcorr_d(const double* x, const double* y, int n, int has_minvar, dou
  * correlation of the unrounded quadratic interpolant, evaluated with the
  * same operations as the CUDA kernel (moments.cu).  mode 0: agree at the
  * integer disparity, out int16 (in place allowed); mode 1: subpixel sweep,
- * out float.  corr: float or double per dbl, may be NULL. */
+ * out float; mode 2: feature rows, out float[8] per pixel (corr unused).
+ * corr: float or double per dbl, may be NULL. */
 void orc_moments(const int16_t* disp, const void* s0, const void* s1, int elem_bytes, int n, int rows,
                  int cols, float thr, float step, int has_minvar, float minvar, int dbl, int mode,
                  void* out, void* corr, int nthreads);
+
+/* Learned subpixel form (extension): mode 2 of orc_moments writes the
+ * network's feature rows (8 floats per pixel).  orc_learned_check restates
+ * the check of the network's proposals: outputs of accepted and border
+ * pixels, fallback[px] = 1 where the sweep decides (out/corr untouched). */
+void orc_learned_check(const int16_t* disp, const void* s0, const void* s1, int elem_bytes, int n, int rows,
+                       int cols, float thr, int has_minvar, float minvar, int dbl, const float* proposal,
+                       const float* features, float drop, float* out, void* corrmap, uint8_t* fallback,
+                       int nthreads);
 
 /* whole pipeline, src/impl/cpu.cpp:96-155 (+ the CUDA build's precision
  * switch).  disp_out: int16 (no step) or float32 (step); corr_out: float32

@@ -264,6 +264,16 @@ def nxcorr_d(x, y, min_var=None):
                               float(min_var or 0.0))
 
 
+def _moments_lib():
+    L = lib()
+    if not getattr(L, "_mom_sig", False):
+        L.orc_moments.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
+                                  C.c_float, C.c_float, C.c_int, C.c_float, C.c_int, C.c_int, C.c_void_p,
+                                  C.c_void_p, C.c_int]
+        L._mom_sig = True
+    return L
+
+
 def moments(disp, stack0, stack1, thr, step=None, min_var_scaled=None, double=True, nthreads=0):
     """Moment form of the agreement (the library's extension): returns
     (int16 disparity, corrmap) without a step, (float disparity, corrmap)
@@ -275,12 +285,46 @@ def moments(disp, stack0, stack1, thr, step=None, min_var_scaled=None, double=Tr
     out = np.empty((rows, cols), np.int16 if mode == 0 else np.float32)
     corr = np.empty((rows, cols), np.float64 if double else np.float32)
     hm = min_var_scaled is not None
-    L = lib()
-    if not getattr(L, "_mom_sig", False):
-        L.orc_moments.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
-                                  C.c_float, C.c_float, C.c_int, C.c_float, C.c_int, C.c_int, C.c_void_p,
-                                  C.c_void_p, C.c_int]
-        L._mom_sig = True
+    L = _moments_lib()
     L.orc_moments(_p(d), _p(s0), _p(s1), s0.dtype.itemsize, n, rows, cols, thr, step or 0.0, int(hm),
                   float(min_var_scaled or 0.0), int(double), mode, _p(out), _p(corr), nthreads)
     return out, corr
+
+
+def features(disp, stack0, stack1, nthreads=0):
+    """Feature rows of the learned subpixel form (orc_moments mode 2):
+    (rows, cols, 8) float32."""
+    s0, s1 = _stack(stack0), _stack(stack1)
+    n, rows, cols = s0.shape
+    d = np.ascontiguousarray(disp, np.int16)
+    out = np.empty((rows, cols, 8), np.float32)
+    L = _moments_lib()
+    L.orc_moments(_p(d), _p(s0), _p(s1), s0.dtype.itemsize, n, rows, cols, 0.0, 0.0, 0, 0.0, 0, 2, _p(out),
+                  None, nthreads)
+    return out
+
+
+def learned_check(disp, stack0, stack1, thr, proposal, feats, min_var_scaled=None, double=False, drop=0.002,
+                  nthreads=0):
+    """The learned form's check of given proposals: (float disparity,
+    corrmap, fallback mask); fallback pixels are NaN here and decided by the
+    sweep (agree_subpixel)."""
+    s0, s1 = _stack(stack0), _stack(stack1)
+    n, rows, cols = s0.shape
+    d = np.ascontiguousarray(disp, np.int16)
+    prop = np.ascontiguousarray(proposal, np.float32)
+    ft = np.ascontiguousarray(feats, np.float32)
+    out = np.empty((rows, cols), np.float32)
+    corr = np.full((rows, cols), np.nan, np.float64 if double else np.float32)
+    fb = np.zeros((rows, cols), np.uint8)
+    hm = min_var_scaled is not None
+    L = lib()
+    if not getattr(L, "_lc_sig", False):
+        L.orc_learned_check.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
+                                        C.c_float, C.c_int, C.c_float, C.c_int, C.c_void_p, C.c_void_p,
+                                        C.c_float, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+        L._lc_sig = True
+    L.orc_learned_check(_p(d), _p(s0), _p(s1), s0.dtype.itemsize, n, rows, cols, thr, int(hm),
+                        float(min_var_scaled or 0.0), int(double), _p(prop), _p(ft), drop, _p(out), _p(corr),
+                        _p(fb), nthreads)
+    return out, corr, fb.astype(bool)
