@@ -155,111 +155,136 @@ __global__ void __launch_bounds__(128) k_agree(const __grid_constant__ AgreePara
         *dp = kInvalidDisp;
 }
 
-// per-frame coefficients of the quadratic through the right columns
-// col1-1, col1, col1+1 (agree.hpp:120-140): a = (y0 - 2 y1 + y2) / 2,
-// b = (y2 - y0) / 2, c = y1, all exact in float
-template<typename T, int NMAX>
-__device__ __forceinline__ void interp_coef(const StackParams& s, int row, int col1, float (&a)[NMAX],
-                                            float (&b)[NMAX], float (&c)[NMAX]) {
-#pragma unroll
-    for (int t = 0; t < NMAX; ++t) {
-        if (t < s.n) {
-            const int y0 = ld_px<T>(s, 1, t, row, col1 - 1);
-            const int y1 = ld_px<T>(s, 1, t, row, col1);
-            const int y2 = ld_px<T>(s, 1, t, row, col1 + 1);
-            a[t] = 0.5f * (float)(y0 - 2 * y1 + y2);
-            b[t] = 0.5f * (float)(y2 - y0);
-            c[t] = (float)y1;
-        } else {
-            a[t] = b[t] = c[t] = 0.f;
-        }
-    }
-}
+constexpr int kListThreads = 128;
 
-// the interpolants at x as the input type: ((a*x)*x + b*x) + c, each step
-// rounded, then round half to even and wrap
-template<typename T, int NMAX>
-__device__ __forceinline__ void interp_at(const float (&a)[NMAX], const float (&b)[NMAX], const float (&c)[NMAX],
-                                          int n, float x, int (&iv)[NMAX]) {
-#pragma unroll
-    for (int t = 0; t < NMAX; ++t) {
-        const float q = __fadd_rn(__fadd_rn(__fmul_rn(__fmul_rn(a[t], x), x), __fmul_rn(b[t], x)), c[t]);
-        iv[t] = t < n ? round_wrap<T>(q) : 0;
-    }
-}
-
-// agree_subpixel of one pixel (agree.hpp:94-185, agree.cuh:161-259),
-// writing its disparity and correlation
-template<typename T, bool DBL, int NMAX>
-__device__ void sweep_pixel(const AgreeParams& p, int row, int col) {
+// The reference sweep (agree.hpp:94-185, agree.cuh:161-259) over the
+// pixels of a list, one warp per pixel.  The warp first stages, per frame,
+// the interpolation coefficients a, b, c of the right columns col1-1..col1+1
+// and the centred left sample d0 = x - mean (position independent, so the
+// same values the sequential sweep forms at every position); lane l then
+// evaluates positions l, l + 32, ... (xs: the sweep's float-accumulated
+// offsets from -1) with the reference's operations in frame order, keeping
+// its first strictly better correlation, and the warp keeps the largest at
+// its first position -- the offset the sequential sweep keeps.  Sums of
+// rounded interpolants are integers below 2^24, exact in float.  Listed
+// pixels are interior matches (1 <= col1 <= cols - 2).
+template<typename T, bool DBL>
+__global__ void __launch_bounds__(kListThreads) k_subpixel_list(const __grid_constant__ AgreeParams p,
+                                                                const int* __restrict__ list,
+                                                                const int* __restrict__ count,
+                                                                const float* __restrict__ xs, int nx) {
     using TP = typename Prec<DBL>::T;
-    const int cols = p.s.cols, n = p.s.n;
-    float result = NAN;
-    TP corr = (TP)NAN;
-    const int16_t d = reinterpret_cast<const int16_t*>(reinterpret_cast<const char*>(p.raw) + row * p.raw_pitch)[col];
-    const int col1 = col - d;
-    if (d != kInvalidDisp && col1 >= 0 && col1 < cols) {
-        int x[NMAX];
+    constexpr int W = kListThreads / 32;
+    __shared__ float4 coef_all[W][kMaxFrames];           // a, b, c, d0 (single precision)
+    __shared__ double d0_all[DBL ? W : 1][kMaxFrames];  // d0 (double precision)
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    float4* coef = coef_all[w];
+    double* d0d = d0_all[DBL ? w : 0];
+    const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
+    const int total = *count, cols = p.s.cols, n = p.s.n;
+    const float fn = (float)n;
+    const bool mv = p.has_minvar != 0;
+    for (int i = warp; i < total; i += nwarps) {
+        const int px = list[i];
+        const int row = px / cols, col = px - row * cols;
+        const int d = reinterpret_cast<const int16_t*>(reinterpret_cast<const char*>(p.raw) + row * p.raw_pitch)[col];
+        const int col1 = col - d;
+        __syncwarp();  // the previous pixel's coefficients are no longer read
+        int xv[3] = {}, sx = 0;
 #pragma unroll
-        for (int t = 0; t < NMAX; ++t)
-            x[t] = t < n ? ld_px<T>(p.s, 0, t, row, col) : 0;
-        const bool mv = p.has_minvar != 0;
-        if (col1 == 0 || col1 == cols - 1) {
-            int y[NMAX];
-#pragma unroll
-            for (int t = 0; t < NMAX; ++t)
-                y[t] = t < n ? ld_px<T>(p.s, 1, t, row, col1) : 0;
-            const TP nxc = nxc_full<DBL>(x, y, n, mv, p.minvar);
-            corr = nxc;
-            if (!(nxc < (TP)p.thr))
-                result = (float)d;
-        } else {
-            float a[NMAX], b[NMAX], c[NMAX];
-            interp_coef<T>(p.s, row, col1, a, b, c);
-            TP d0[NMAX], var0;
-            if constexpr (DBL)
-                left_d(x, n, d0, var0);
-            else
-                left_f(x, n, d0, var0);
-
-            float best_x = 0.f;
-            TP best = (TP)-1.0;
-            for (float xs = -1.f; xs <= 1.f; xs = __fadd_rn(xs, p.step)) {
-                int iv[NMAX];
-                interp_at<T>(a, b, c, n, xs, iv);
-                TP nxc;
-                if constexpr (DBL)
-                    nxc = nxc_d(d0, var0, iv, n, mv, (double)p.minvar);
-                else
-                    nxc = nxc_f(d0, var0, iv, n, mv, p.minvar);
-                if (best < nxc) {
-                    best_x = xs;
-                    best = nxc;
-                }
+        for (int r = 0; r < 3; ++r) {  // frames lane, lane + 32, lane + 64 (n <= 65)
+            const int t = lane + 32 * r;
+            if (t < n) {
+                const int y0 = ld_px<T>(p.s, 1, t, row, col1 - 1);
+                const int y1 = ld_px<T>(p.s, 1, t, row, col1);
+                const int y2 = ld_px<T>(p.s, 1, t, row, col1 + 1);
+                xv[r] = ld_px<T>(p.s, 0, t, row, col);
+                sx += xv[r];
+                coef[t] = make_float4(0.5f * (float)(y0 - 2 * y1 + y2), 0.5f * (float)(y2 - y0), (float)y1, 0.f);
             }
-            corr = best;
-            if (!(best < (TP)p.thr))
-                result = __fsub_rn((float)d, best_x);
+        }
+        sx = __reduce_add_sync(0xffffffffu, sx);  // integer sum: exact in any order
+        TP var0 = 0;
+        if constexpr (DBL) {
+            const double m0 = __ddiv_rn((double)sx, (double)n);
+#pragma unroll
+            for (int r = 0; r < 3; ++r)
+                if (lane + 32 * r < n)
+                    d0d[lane + 32 * r] = __dsub_rn((double)xv[r], m0);
+            __syncwarp();
+            for (int t = 0; t < n; ++t)
+                var0 = __fma_rn(d0d[t], d0d[t], var0);
+        } else {
+            const float m0 = __fdiv_rn((float)sx, fn);
+#pragma unroll
+            for (int r = 0; r < 3; ++r)
+                if (lane + 32 * r < n)
+                    coef[lane + 32 * r].w = __fsub_rn((float)xv[r], m0);
+            __syncwarp();
+            for (int t = 0; t < n; ++t)
+                var0 = __fmaf_rn(coef[t].w, coef[t].w, var0);
+        }
+        TP best = (TP)-1.0;
+        int bk = -1;
+        for (int k = lane; k < nx; k += 32) {
+            const float x = xs[k];
+            float sy = 0.f;
+#pragma unroll 4
+            for (int t = 0; t < n; ++t) {
+                const float4 c = coef[t];
+                sy = __fadd_rn(sy, round_wrap_f<T>(__fadd_rn(__fadd_rn(__fmul_rn(__fmul_rn(c.x, x), x), __fmul_rn(c.y, x)), c.z)));
+            }
+            TP cov = 0, var1 = 0, r;
+            if constexpr (DBL) {
+                const double m1 = __ddiv_rn((double)sy, (double)n);
+#pragma unroll 4
+                for (int t = 0; t < n; ++t) {
+                    const float4 c = coef[t];
+                    const float v = round_wrap_f<T>(__fadd_rn(__fadd_rn(__fmul_rn(__fmul_rn(c.x, x), x), __fmul_rn(c.y, x)), c.z));
+                    const double d1 = __dsub_rn((double)v, m1);
+                    cov = __fma_rn(d0d[t], d1, cov);
+                    var1 = __fma_rn(d1, d1, var1);
+                }
+                r = (mv && (var0 < (double)p.minvar || var1 < (double)p.minvar))
+                        ? -1.0 : __ddiv_rn(cov, __dsqrt_rn(__dmul_rn(var0, var1)));
+            } else {
+                const float m1 = __fdiv_rn(sy, fn);
+#pragma unroll 4
+                for (int t = 0; t < n; ++t) {
+                    const float4 c = coef[t];
+                    const float v = round_wrap_f<T>(__fadd_rn(__fadd_rn(__fmul_rn(__fmul_rn(c.x, x), x), __fmul_rn(c.y, x)), c.z));
+                    const float d1 = __fsub_rn(v, m1);
+                    cov = __fmaf_rn(c.w, d1, cov);
+                    var1 = __fmaf_rn(d1, d1, var1);
+                }
+                r = (mv && (var0 < p.minvar || var1 < p.minvar)) ? -1.f
+                                                                   : __fdiv_rn(cov, __fsqrt_rn(__fmul_rn(var0, var1)));
+            }
+            if (best < r) {
+                best = r;
+                bk = k;
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const TP ob = __shfl_xor_sync(0xffffffffu, best, o);
+            const int ok = __shfl_xor_sync(0xffffffffu, bk, o);
+            if (ok >= 0 && (bk < 0 || best < ob || (ob == best && ok < bk))) {
+                best = ob;
+                bk = ok;
+            }
+        }
+        if (lane == 0) {
+            const float bx = bk >= 0 ? xs[bk] : 0.f;
+            reinterpret_cast<float*>(reinterpret_cast<char*>(p.out) + row * p.out_pitch)[col] =
+                !(best < (TP)p.thr) ? __fsub_rn((float)d, bx) : NAN;
+            put_corr<TP>(p, row, col, best);
         }
     }
-    reinterpret_cast<float*>(reinterpret_cast<char*>(p.out) + row * p.out_pitch)[col] = result;
-    put_corr<TP>(p, row, col, corr);
 }
 
-// the sweep over the pixels of a list (the learned form's fallback);
-// grid-stride over a length that only the device knows
-template<typename T, bool DBL, int NMAX>
-__global__ void __launch_bounds__(128) k_subpixel_list(const __grid_constant__ AgreeParams p,
-                                                       const int* __restrict__ list, const int* __restrict__ count) {
-    const int total = *count;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
-        const int px = list[i];
-        sweep_pixel<T, DBL, NMAX>(p, px / p.s.cols, px % p.s.cols);
-    }
-}
-
-// Single-precision subpixel sweep, same results as sweep_pixel<T, false,
-// NMAX> over every pixel, organised for throughput:
+// Single-precision subpixel sweep (agree.hpp:94-185), organised for throughput:
 //  - per pixel, the frame coefficients (a, b, c) and the centred left
 //    samples d0 are staged once in shared memory as one float4 per frame
 //    (each thread reads back only its own column, so no barrier is needed);
@@ -274,13 +299,6 @@ __global__ void __launch_bounds__(128) k_subpixel_list(const __grid_constant__ A
 //    2^23 exponent trick: the value of (T)__float2int_rn(q) without any
 //    conversion instruction;
 constexpr int kSubThreads = 64;
-
-template<typename T>
-__device__ __forceinline__ float round_wrap_f(float q) {
-    constexpr uint32_t kMask = sizeof(T) == 1 ? 0xFFu : 0xFFFFu;
-    const float f = __fadd_rn(q, 12582912.0f);
-    return __fsub_rn(__uint_as_float((__float_as_uint(f) & kMask) | 0x4B000000u), 8388608.0f);
-}
 
 __device__ __forceinline__ float nxc_from(float cov, float var0, float var1, bool mv, float minvar) {
     return (mv && (var0 < minvar || var1 < minvar)) ? -1.f : __fdiv_rn(cov, __fsqrt_rn(__fmul_rn(var0, var1)));
@@ -404,8 +422,8 @@ __global__ void __launch_bounds__(kSubThreads) k_subpixel_f32(const __grid_const
     put_corr<float>(p, row, col, corr);
 }
 
-// Double-precision subpixel sweep, same results as sweep_pixel<T,
-// true, NMAX> (the reference's nxcorrd, include/impl/cuda/agree.cuh:35-65),
+// Double-precision subpixel sweep (the reference's nxcorrd,
+// include/impl/cuda/agree.cuh:35-65, in agree.cuh:161-259),
 // with FP64 work only where it can decide the result:
 //  - one pass over the sweep forms, per point, the exact integer moments
 //    Sy, Syy, Sxy of the rounded interpolants and an FP32 estimate
@@ -664,37 +682,28 @@ cudaError_t launch_any(const AgreeParams& p, bool dbl, cudaStream_t st) {
 }
 
 template<typename T, bool DBL>
-cudaError_t launch_list_t(const AgreeParams& p, const int* list, const int* count, cudaStream_t st) {
+cudaError_t launch_list_t(const AgreeParams& p, const int* list, const int* count, const float* xs, int nx,
+                          cudaStream_t st) {
     int dev = 0, sms = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess)
         e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess)
         return e;
-    const int blocks = sms * 8;  // grid-stride; the list length is known on the device only
-    const int n = p.s.n;
-#define BICOS_LIST_CASE(NM)                                                    \
-    if (n <= NM) {                                                             \
-        k_subpixel_list<T, DBL, NM><<<blocks, 128, 0, st>>>(p, list, count); \
-        return cudaGetLastError();                                             \
-    }
-    BICOS_LIST_CASE(8)
-    BICOS_LIST_CASE(16)
-    BICOS_LIST_CASE(24)
-    BICOS_LIST_CASE(33)
-    BICOS_LIST_CASE(48)
-    BICOS_LIST_CASE(65)
-#undef BICOS_LIST_CASE
-    return cudaErrorInvalidValue;
+    // grid-stride over a list whose length only the device knows
+    k_subpixel_list<T, DBL><<<sms * 16, kListThreads, 0, st>>>(p, list, count, xs, nx);
+    return cudaGetLastError();
 }
 
 }  // namespace
 
 cudaError_t launch_subpixel_list(const AgreeParams& p, bool dbl, const int* list, const int* count,
-                                 cudaStream_t st) {
+                                 const float* xs, int nx, cudaStream_t st) {
     if (p.s.elem_bytes == 1)
-        return dbl ? launch_list_t<uint8_t, true>(p, list, count, st) : launch_list_t<uint8_t, false>(p, list, count, st);
-    return dbl ? launch_list_t<uint16_t, true>(p, list, count, st) : launch_list_t<uint16_t, false>(p, list, count, st);
+        return dbl ? launch_list_t<uint8_t, true>(p, list, count, xs, nx, st)
+                   : launch_list_t<uint8_t, false>(p, list, count, xs, nx, st);
+    return dbl ? launch_list_t<uint16_t, true>(p, list, count, xs, nx, st)
+               : launch_list_t<uint16_t, false>(p, list, count, xs, nx, st);
 }
 
 cudaError_t launch_agree(const AgreeParams& p, bool dbl, cudaStream_t st) {

@@ -13,6 +13,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "../../include/bicos_c.h"
 #include "kernels.cuh"
@@ -200,14 +201,36 @@ struct DeviceGuard {
 // the learned form accepts a proposal when rho(x) >= rho(0) - kLearnedDrop
 constexpr float kLearnedDrop = 0.002f;
 
-// scratch of the learned form: the fallback list (one int per pixel) and
-// its length
-size_t learned_scratch_bytes(size_t px) { return align_up(px * 4, 256) + 256; }
+// the sweep's offsets: -1, then float-accumulated steps while <= 1
+// (agree.hpp:142-143; the same sequence on every IEEE host)
+std::vector<float> sweep_offsets(float step) {
+    std::vector<float> xs;
+    for (float x = -1.f; x <= 1.f; x += step)
+        xs.push_back(x);
+    return xs;
+}
+
+// scratch of the learned form: the fallback list (one int per pixel), its
+// length, the sweep's offsets (step >= 1e-4: at most 20001 of them)
+constexpr size_t kMaxOffsets = 20480;
+size_t learned_scratch_bytes(size_t px) { return align_up(px * 4, 256) + 256 + kMaxOffsets * 4; }
+
+// 16-byte loads of whole rows are possible: frames and pitches 16-byte
+// aligned, row width a multiple of 16 bytes
+bool frames_vec16(const StackParams& s) {
+    if ((s.cols * s.elem_bytes) % 16 != 0)
+        return false;
+    for (int side = 0; side < 2; ++side)
+        for (int t = 0; t < s.n; ++t)
+            if (reinterpret_cast<uintptr_t>(s.frame[side][t]) % 16 != 0 || s.pitch[side][t] % 16 != 0)
+                return false;
+    return true;
+}
 
 // Learned subpixel stage: one fused pass (features -> network -> one
 // reference NCC check per pixel), then the reference sweep over the pixels
-// whose check failed.  `ap` carries the raw disparity, the float output and
-// the corrmap; `scratch` holds learned_scratch_bytes(px).
+// whose check failed.  `ap` carries the raw disparity, the float output,
+// the corrmap and the sweep step; `scratch` holds learned_scratch_bytes(px).
 cudaError_t learned_subpixel(const AgreeParams& ap, bool dbl, const float* model, void* scratch,
                              int* fallback_count_out, float* proposal, long long proposal_pitch,
                              cudaStream_t st) {
@@ -215,7 +238,13 @@ cudaError_t learned_subpixel(const AgreeParams& ap, bool dbl, const float* model
     char* b = static_cast<char*>(scratch);
     int* list = reinterpret_cast<int*>(b);
     int* count = reinterpret_cast<int*>(b + align_up(px * 4, 256));
-    cudaError_t e = cudaMemsetAsync(count, 0, sizeof(int), st);
+    float* xs = reinterpret_cast<float*>(b + align_up(px * 4, 256) + 256);
+    const std::vector<float> offsets = sweep_offsets(ap.step);
+    if (offsets.size() > kMaxOffsets)
+        return cudaErrorInvalidValue;
+    cudaError_t e = cudaMemcpyAsync(xs, offsets.data(), offsets.size() * 4, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(count, 0, 2 * sizeof(int), st);  // list length and tile counter
     if (e == cudaSuccess) {
         LearnedParams lp;
         std::memset(&lp, 0, sizeof lp);
@@ -225,11 +254,13 @@ cudaError_t learned_subpixel(const AgreeParams& ap, bool dbl, const float* model
         lp.proposal_pitch = proposal_pitch;
         lp.list = list;
         lp.count = count;
+        lp.tile_counter = count + 1;
         lp.drop = kLearnedDrop;
+        lp.vec16 = frames_vec16(ap.s) ? 1 : 0;
         e = launch_learned(lp, dbl, st);
     }
     if (e == cudaSuccess)
-        e = launch_subpixel_list(ap, dbl, list, count, st);
+        e = launch_subpixel_list(ap, dbl, list, count, xs, (int)offsets.size(), st);
     if (e == cudaSuccess && fallback_count_out)
         e = cudaMemcpyAsync(fallback_count_out, count, sizeof(int), cudaMemcpyDeviceToHost, st);
     return e;

@@ -95,12 +95,15 @@ struct LearnedParams {
     long long proposal_pitch;
     int* list;                 // pixels (row * cols + col) left to the sweep
     int* count;                // length of list, zeroed before the launch
+    int* tile_counter;         // tiles claimed so far, zeroed before the launch
     float drop;                // accepted when rho(x) >= rho(0) - drop
+    int vec16;                 // frames 16-byte aligned with 16-byte pitches and row widths
 };
 cudaError_t launch_learned(const LearnedParams& p, bool dbl, cudaStream_t st);
-// the reference sweep over the pixels of a list (agree.cu)
+// the reference sweep over the pixels of a list (agree.cu); xs: the sweep's
+// nx offsets (-1, then float-accumulated steps while <= 1)
 cudaError_t launch_subpixel_list(const AgreeParams& p, bool dbl, const int* list, const int* count,
-                                 cudaStream_t st);
+                                 const float* xs, int nx, cudaStream_t st);
 
 // subpixel network (learned.cu); a model buffer holds mlp_model_floats()
 // floats: the parameters, then the input means and standard deviations

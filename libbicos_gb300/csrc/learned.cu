@@ -29,6 +29,7 @@
 //   k_learned      the matcher's stage: features, network and NCC check
 //                  per pixel in one persistent pass over 128-pixel tiles
 #include <cuda_bf16.h>
+#include <limits.h>
 #include <math.h>
 #include <string.h>
 
@@ -66,6 +67,11 @@ __device__ __forceinline__ float tanh_fast(float u) {
 }
 
 __device__ __forceinline__ float gelu_arg(float z) { return kGeluC * fmaf(kGeluA * z, z * z, z); }
+// inference form: 0.5 z + 0.5 z tanh(z (c + c a z^2)), hardware tanh
+__device__ __forceinline__ float gelu_fast(float z) {
+    const float hz = 0.5f * z;
+    return fmaf(hz, tanh_fast(z * fmaf(kGeluC * kGeluA, z * z, kGeluC)), hz);
+}
 __device__ __forceinline__ float gelu_from(float z, float t) { return 0.5f * z * (1.f + t); }
 __device__ __forceinline__ float gelu_grad_from(float z, float t) {
     return 0.5f * (1.f + t) + 0.5f * z * (1.f - t * t) * kGeluC * fmaf(3.f * kGeluA, z * z, 1.f);
@@ -336,7 +342,8 @@ struct InferSmem {
     // layout with kBChunk.
     alignas(128) uint8_t a[kRowsPT * kH * 2];
     alignas(128) uint8_t b[kH * kH * 2];
-    float w1[kH * kIn], b1[kH], b2[kH], w3[kH];
+    float4 w1[kH][2];  // unit j: its 7 input weights, then its bias
+    float2 bw[kH];     // unit j of layer 2: bias, output weight
     float norm[2 * kIn];
     float b3;
     alignas(8) uint64_t mbar;
@@ -356,12 +363,11 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
 __device__ void infer_setup(InferSmem& S, const float* __restrict__ model) {
     using namespace tc;
     const int tid = threadIdx.x;
-    for (int i = tid; i < kH * kIn; i += kRowsPT)
-        S.w1[i] = bf16r(model[kW1 + i]);
-    for (int i = tid; i < kH; i += kRowsPT) {
-        S.b1[i] = bf16r(model[kB1 + i]);
-        S.b2[i] = bf16r(model[kB2 + i]);
-        S.w3[i] = bf16r(model[kW3 + i]);
+    for (int j = tid; j < kH; j += kRowsPT) {
+        const float* w = model + kW1 + j * kIn;
+        S.w1[j][0] = make_float4(bf16r(w[0]), bf16r(w[1]), bf16r(w[2]), bf16r(w[3]));
+        S.w1[j][1] = make_float4(bf16r(w[4]), bf16r(w[5]), bf16r(w[6]), bf16r(model[kB1 + j]));
+        S.bw[j] = make_float2(bf16r(model[kB2 + j]), bf16r(model[kW3 + j]));
     }
     if (tid < 2 * kIn)
         S.norm[tid] = model[kNorm + tid];
@@ -412,11 +418,16 @@ __device__ bool infer_tile(InferSmem& S, const float (&x)[kIn], uint32_t phase, 
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
             const int j = c * 8 + q;
-            float z = S.b1[j];
-#pragma unroll
-            for (int i = 0; i < kIn; ++i)
-                z = fmaf(S.w1[j * kIn + i], x[i], z);
-            h[q] = gelu_from(z, tanh_fast(gelu_arg(z)));
+            const float4 wa = S.w1[j][0], wb = S.w1[j][1];
+            float z = wb.w;
+            z = fmaf(wa.x, x[0], z);
+            z = fmaf(wa.y, x[1], z);
+            z = fmaf(wa.z, x[2], z);
+            z = fmaf(wa.w, x[3], z);
+            z = fmaf(wb.x, x[4], z);
+            z = fmaf(wb.y, x[5], z);
+            z = fmaf(wb.z, x[6], z);
+            h[q] = gelu_fast(z);
         }
         *reinterpret_cast<uint4*>(S.a + c * kAChunk + tid * 16) =
             make_uint4(pack_bf16(h[0], h[1]), pack_bf16(h[2], h[3]), pack_bf16(h[4], h[5]), pack_bf16(h[6], h[7]));
@@ -446,9 +457,9 @@ __device__ bool infer_tile(InferSmem& S, const float (&x)[kIn], uint32_t phase, 
         tmem_ld32(S.tmem + ((uint32_t)(warp * 32) << 16) + half * 32, v);
 #pragma unroll
         for (int k = 0; k < 32; ++k) {
-            const int j = half * 32 + k;
-            const float z = v[k] + S.b2[j];
-            acc = fmaf(S.w3[j], gelu_from(z, tanh_fast(gelu_arg(z))), acc);
+            const float2 bw = S.bw[half * 32 + k];
+            const float z = v[k] + bw.x;
+            acc = fmaf(bw.y, gelu_fast(z), acc);
         }
     }
     *y = tanhf(acc);
@@ -489,21 +500,18 @@ __global__ void __launch_bounds__(kRowsPT) k_mlp_propose(const float* __restrict
 // Feature row of one interior match, the same values as the moment
 // kernel's mode 2 (moments.cu): exact integer sums over the frames of the
 // left pixel and of the right columns col1-2..col1+2, then FP32 ratios.
-template<typename T>
-__device__ __forceinline__ void pixel_features(const StackParams& s, int row, int col, int col1, float (&f)[8]) {
+template<typename T, typename Row>
+__device__ __forceinline__ void pixel_features(const Row& src, int n, int cols, int col, int col1, float (&f)[8]) {
     using Acc = typename std::conditional<sizeof(T) == 1, int, long long>::type;
     Acc sx = 0, sxx = 0, sy[5] = {}, syy[5] = {}, sxy[5] = {};
-    const int cols = s.cols, n = s.n;
     for (int t = 0; t < n; ++t) {
-        const T* lr = reinterpret_cast<const T*>(s.frame[0][t] + (long long)row * s.pitch[0][t]);
-        const T* rr = reinterpret_cast<const T*>(s.frame[1][t] + (long long)row * s.pitch[1][t]);
-        const Acc x = (Acc)__ldg(lr + col);
+        const Acc x = (Acc)src.left(t, col);
         sx += x;
         sxx += x * x;
 #pragma unroll
         for (int j = 0; j < 5; ++j) {
             const int c = col1 + j - 2;
-            const Acc y = (c >= 0 && c < cols) ? (Acc)__ldg(rr + c) : (Acc)0;
+            const Acc y = (c >= 0 && c < cols) ? (Acc)src.right(t, c) : (Acc)0;
             sy[j] += y;
             syy[j] += y * y;
             sxy[j] += x * y;
@@ -529,6 +537,155 @@ __device__ __forceinline__ void pixel_features(const StackParams& s, int row, in
     f[7] = 1.f;
 }
 
+// The same features from the tile's shared-memory copy: lp points at the
+// left sample of frame 0 (frames kRowsPT apart), rp at the right column col1
+// of frame 0 (frames rstride apart); bit j of okm: column col1-2+j is inside
+// the image (outside ones read column col1 and count as 0).  Also returns
+// the left sum.
+template<typename T>
+__device__ __forceinline__ int features_staged(const T* __restrict__ lp, const T* __restrict__ rp, int n,
+                                               int rstride, int okm, float (&f)[8]) {
+    using Acc = typename std::conditional<sizeof(T) == 1, int, long long>::type;
+    int off[5];
+    Acc m[5];
+#pragma unroll
+    for (int j = 0; j < 5; ++j) {
+        const bool ok = (okm >> j) & 1;
+        off[j] = ok ? j - 2 : 0;
+        m[j] = ok ? 1 : 0;
+    }
+    Acc sx = 0, sxx = 0, sy[5] = {}, syy[5] = {}, sxy[5] = {};
+    if (okm == 31) {  // all five columns inside the image
+#pragma unroll 2
+        for (int t = 0; t < n; ++t, lp += kRowsPT, rp += rstride) {
+            const Acc x = (Acc)lp[0];
+            sx += x;
+            sxx += x * x;
+#pragma unroll
+            for (int j = 0; j < 5; ++j) {
+                const Acc y = (Acc)rp[j - 2];
+                sy[j] += y;
+                syy[j] += y * y;
+                sxy[j] += x * y;
+            }
+        }
+    } else {
+        for (int t = 0; t < n; ++t, lp += kRowsPT, rp += rstride) {
+            const Acc x = (Acc)lp[0];
+            sx += x;
+            sxx += x * x;
+#pragma unroll
+            for (int j = 0; j < 5; ++j) {
+                const Acc y = (Acc)rp[off[j]] * m[j];
+                sy[j] += y;
+                syy[j] += y * y;
+                sxy[j] += x * y;
+            }
+        }
+    }
+    const long long nn = n;
+    const long long v0 = nn * (long long)sxx - (long long)sx * (long long)sx;
+    const float fv0 = __ll2float_rn(v0);
+#pragma unroll
+    for (int j = 0; j < 5; ++j) {
+        if ((okm >> j) & 1) {
+            const long long v1 = nn * (long long)syy[j] - (long long)sy[j] * (long long)sy[j];
+            const long long num = nn * (long long)sxy[j] - (long long)sx * (long long)sy[j];
+            f[j] = __fdiv_rn(__ll2float_rn(num), __fsqrt_rn(__fmul_rn(fv0, __ll2float_rn(v1))));
+        } else {
+            f[j] = NAN;
+        }
+    }
+    const float n2 = __fmul_rn((float)n, (float)n);
+    f[5] = __fdiv_rn(fv0, n2);
+    f[6] = __fdiv_rn(__ll2float_rn(nn * (long long)syy[2] - (long long)sy[2] * (long long)sy[2]), n2);
+    f[7] = 1.f;
+    return (int)sx;
+}
+
+// The reference NCC at offset x (nxc_row<T, DBL, true>, same operations in
+// the same order) from the tile's shared-memory copy, with the left sum sx
+// known and the rounded interpolants of the first pass kept in iv (this
+// thread's column, frames kRowsPT apart) for the second.
+template<typename T, bool DBL>
+__device__ __forceinline__ typename Prec<DBL>::T check_staged(const T* __restrict__ lp, const T* __restrict__ rp,
+                                                               T* __restrict__ iv, int n, int rstride, int sx,
+                                                               float x, bool mv, float minvar) {
+    int sy = 0;
+    {
+        const T* r = rp;
+        T* v = iv;
+#pragma unroll 2
+        for (int t = 0; t < n; ++t, r += rstride, v += kRowsPT) {
+            const int y0 = r[-1], y1 = r[0], y2 = r[1];
+            const float a = 0.5f * small_int_to_float(y0 - 2 * y1 + y2), b = 0.5f * small_int_to_float(y2 - y0),
+                        c = small_int_to_float(y1);
+            const int q = round_wrap_bits<T>(__fadd_rn(__fadd_rn(__fmul_rn(__fmul_rn(a, x), x), __fmul_rn(b, x)), c));
+            *v = (T)q;
+            sy += q;
+        }
+    }
+    if constexpr (DBL) {
+        double cov = 0, var0 = 0, var1 = 0;
+        const double m0 = __ddiv_rn((double)sx, (double)n), m1 = __ddiv_rn((double)sy, (double)n);
+        for (int t = 0; t < n; ++t, lp += kRowsPT, iv += kRowsPT) {
+            const double d0 = __dsub_rn((double)(int)lp[0], m0);
+            const double d1 = __dsub_rn((double)(int)iv[0], m1);
+            var0 = __fma_rn(d0, d0, var0);
+            cov = __fma_rn(d0, d1, cov);
+            var1 = __fma_rn(d1, d1, var1);
+        }
+        if (mv && (var0 < (double)minvar || var1 < (double)minvar))
+            return -1.0;
+        return __ddiv_rn(cov, __dsqrt_rn(__dmul_rn(var0, var1)));
+    } else {
+        float cov = 0, var0 = 0, var1 = 0;
+        const float m0 = __fdiv_rn((float)sx, (float)n), m1 = __fdiv_rn((float)sy, (float)n);
+#pragma unroll 2
+        for (int t = 0; t < n; ++t, lp += kRowsPT, iv += kRowsPT) {
+            const float d0 = __fsub_rn(small_int_to_float(lp[0]), m0);
+            const float d1 = __fsub_rn(small_int_to_float(iv[0]), m1);
+            var0 = __fmaf_rn(d0, d0, var0);
+            cov = __fmaf_rn(d0, d1, cov);
+            var1 = __fmaf_rn(d1, d1, var1);
+        }
+        if (mv && (var0 < minvar || var1 < minvar))
+            return -1.f;
+        return __fdiv_rn(cov, __fsqrt_rn(__fmul_rn(var0, var1)));
+    }
+}
+
+constexpr int kWin = 256;  // right-window columns one tile may stage
+
+// shared-memory copy of frames' columns [c0, c1) of one row, row stride
+// `stride` elements; 16-byte loads when the frames allow them
+template<typename T>
+__device__ __forceinline__ void stage_rows(const StackParams& s, int side, int row, int c0, int c1, T* dst,
+                                           int stride, bool vec16) {
+    const int n = s.n;
+    if (vec16) {
+        const int chunks = (c1 - c0) * (int)sizeof(T) / 16;
+        for (int e = threadIdx.x; e < n * chunks; e += blockDim.x) {
+            const int t = e / chunks, k = e - t * chunks;
+            const uint8_t* src = s.frame[side][t] + (long long)row * s.pitch[side][t] + (long long)c0 * sizeof(T);
+            *reinterpret_cast<uint4*>(reinterpret_cast<uint8_t*>(dst + t * stride) + k * 16) =
+                __ldg(reinterpret_cast<const uint4*>(src) + k);
+        }
+    } else {
+        const int w = c1 - c0;
+        for (int e = threadIdx.x; e < n * w; e += blockDim.x) {
+            const int t = e / w, k = e - t * w;
+            dst[t * stride + k] = __ldg(reinterpret_cast<const T*>(s.frame[side][t] + (long long)row * s.pitch[side][t]) + c0 + k);
+        }
+    }
+}
+
+template<typename T>
+constexpr int stage_rstride() { return kWin + 32 / (int)sizeof(T); }
+
+template<typename T>
+size_t stage_bytes(int n) { return (size_t)n * sizeof(T) * (kRowsPT + stage_rstride<T>()); }
+
 // The learned agreement stage in one pass over 128-pixel row tiles: per
 // pixel the features, the network's offset x (tensor cores for the 64x64
 // layer), and one NCC evaluation in the reference's arithmetic at x; the
@@ -537,21 +694,42 @@ __device__ __forceinline__ void pixel_features(const StackParams& s, int row, in
 // NaN below the threshold); otherwise the pixel joins the list for the
 // reference sweep.  Border pixels (col1 = 0 or cols - 1) take the plain
 // correlation at col1, as in the sweep (agree.hpp:110-118).
+//
+// Each tile first copies its left columns and the right columns its
+// matches need (at most kWin wide) of every frame into shared memory, so
+// the three passes over the frames read shared memory; a tile whose
+// matches spread wider reads the frames from global memory instead.
 template<typename T, bool DBL>
 __global__ void __launch_bounds__(kRowsPT) k_learned(const __grid_constant__ LearnedParams lp) {
     using TP = typename Prec<DBL>::T;
     __shared__ InferSmem S;
+    __shared__ int red[2][kRowsPT / 32];
+    extern __shared__ __align__(16) uint8_t stage[];
+    constexpr int rstride = stage_rstride<T>();
     infer_setup(S, lp.model);
     const AgreeParams& p = lp.a;
     const StackParams& s = p.s;
-    const int cols = s.cols;
+    const int cols = s.cols, n = s.n;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const bool mv = p.has_minvar != 0;
+    T* Ls = reinterpret_cast<T*>(stage);
+    T* Rs = Ls + n * kRowsPT;
     const int per_row = (cols + kRowsPT - 1) / kRowsPT;
-    const long long tiles = (long long)s.rows * per_row;
+    const int tiles = s.rows * per_row;
+    __shared__ int next_tile;
     uint32_t phase = 0;
-    for (long long tile = blockIdx.x; tile < tiles; tile += gridDim.x, phase ^= 1u) {
-        const int row = (int)(tile / per_row);
-        const int col = (int)(tile % per_row) * kRowsPT + (int)threadIdx.x;
+    for (;; phase ^= 1u) {
+        // tiles are claimed from a global counter, so every resident CTA
+        // keeps working however many the SMs hold
+        __syncthreads();  // the previous tile is done with the staged rows and next_tile
+        if (threadIdx.x == 0)
+            next_tile = atomicAdd(lp.tile_counter, 1);
+        __syncthreads();
+        const int tile = next_tile;
+        if (tile >= tiles)
+            break;
+        const int row = tile / per_row;
+        const int c0 = (tile - row * per_row) * kRowsPT, col = c0 + (int)threadIdx.x;
         int kind = 0;  // 0: no match, 1: border, 2: interior
         int d = 0, col1 = 0;
         if (col < cols) {
@@ -560,13 +738,56 @@ __global__ void __launch_bounds__(kRowsPT) k_learned(const __grid_constant__ Lea
             if (d != kInvalidDisp && col1 >= 0 && col1 < cols)
                 kind = (col1 == 0 || col1 == cols - 1) ? 1 : 2;
         }
+        // the right columns this tile's matches read
+        int need_lo = INT_MAX, need_hi = INT_MIN;
+        if (kind == 2) {
+            need_lo = max(col1 - 2, 0);
+            need_hi = min(col1 + 2, cols - 1);
+        } else if (kind == 1) {
+            need_lo = need_hi = col1;
+        }
+        need_lo = __reduce_min_sync(0xffffffffu, need_lo);
+        need_hi = __reduce_max_sync(0xffffffffu, need_hi);
+        if (lane == 0) {
+            red[0][warp] = need_lo;
+            red[1][warp] = need_hi;
+        }
+        __syncthreads();
+        int lo = red[0][0], hi = red[1][0];
+#pragma unroll
+        for (int w = 1; w < kRowsPT / 32; ++w) {
+            lo = min(lo, red[0][w]);
+            hi = max(hi, red[1][w]);
+        }
+        int r0 = lo, r1 = hi + 1;
+        if (lp.vec16 && lo <= hi) {
+            r0 = ((lo * (int)sizeof(T)) & ~15) / (int)sizeof(T);
+            r1 = min((((r1 * (int)sizeof(T)) + 15) & ~15) / (int)sizeof(T), cols);
+        }
+        const bool staged = lo > hi || r1 - r0 <= rstride;
+        if (staged && lo <= hi) {
+            stage_rows<T>(s, 0, row, c0, min(c0 + kRowsPT, cols), Ls, kRowsPT, lp.vec16);
+            stage_rows<T>(s, 1, row, r0, r1, Rs, rstride, lp.vec16);
+        }
+        __syncthreads();
+        const SharedRow<T> sh{Ls, Rs, kRowsPT, rstride, c0, r0};
+        const GlobalRow<T> gl{&s, row};
+
+        const T* lcol = Ls + (col - c0);
+        const T* rcol = Rs + (col1 - r0);
         float x[kIn] = {};
-        float r0 = NAN;
+        float r0f = NAN;
+        int sx = 0;
         if (kind == 2) {
             float f[8];
-            pixel_features<T>(s, row, col, col1, f);
+            if (staged) {
+                const int okm = (col1 >= 2 ? 1 : 0) | 2 | 4 | 8 | (col1 + 2 < cols ? 16 : 0);
+                sx = features_staged<T>(lcol, rcol, n, rstride, okm, f);
+            } else {
+                pixel_features<T>(gl, n, cols, col, col1, f);
+            }
             net_inputs(f, S.norm, x);
-            r0 = f[2];
+            r0f = f[2];
         }
         float xo;
         if (!infer_tile(S, x, phase, &xo))
@@ -577,16 +798,24 @@ __global__ void __launch_bounds__(kRowsPT) k_learned(const __grid_constant__ Lea
         TP corr = (TP)NAN;
         bool fallback = false;
         if (kind == 1) {
-            corr = nxc_stream<T, DBL, false>(s, row, col, col1, 0.f, mv, p.minvar);
+            corr = staged ? nxc_row<T, DBL, false>(sh, n, col, col1, 0.f, mv, p.minvar)
+                          : nxc_row<T, DBL, false>(gl, n, col, col1, 0.f, mv, p.minvar);
             if (!(corr < (TP)p.thr))
                 result = (float)d;
         } else if (kind == 2) {
-            const TP nxc = nxc_stream<T, DBL, true>(s, row, col, col1, xo, mv, p.minvar);
+            // the A tile is free once the MMA has completed: it holds the
+            // rounded interpolants between the check's two passes
+            const bool iv_fits = n * (int)sizeof(T) * kRowsPT <= (int)sizeof(S.a);
+            const TP nxc = staged && iv_fits
+                               ? check_staged<T, DBL>(lcol, rcol, reinterpret_cast<T*>(S.a) + threadIdx.x, n, rstride,
+                                                      sx, xo, mv, p.minvar)
+                           : staged ? nxc_row<T, DBL, true>(sh, n, col, col1, xo, mv, p.minvar)
+                                    : nxc_row<T, DBL, true>(gl, n, col, col1, xo, mv, p.minvar);
             TP floor_rho;
             if constexpr (DBL)
-                floor_rho = __dsub_rn((double)r0, (double)lp.drop);
+                floor_rho = __dsub_rn((double)r0f, (double)lp.drop);
             else
-                floor_rho = __fsub_rn(r0, lp.drop);
+                floor_rho = __fsub_rn(r0f, lp.drop);
             if (nxc >= floor_rho) {
                 corr = nxc;
                 if (!(nxc < (TP)p.thr))
@@ -735,25 +964,31 @@ cudaError_t launch_mlp_propose(const float* model, const float* features, int co
     return cudaGetLastError();
 }
 
+template<typename T, bool DBL>
+cudaError_t launch_learned_t(const LearnedParams& p, int sms, cudaStream_t st) {
+    auto k = k_learned<T, DBL>;
+    const size_t smem = stage_bytes<T>(p.a.s.n);
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+    if (e != cudaSuccess)
+        return e;
+    // at most kInferCtas CTAs fit an SM (TMEM); CTAs beyond what the SM
+    // holds start when others finish and find the tile counter exhausted
+    const int tiles = p.a.s.rows * ((p.a.s.cols + kRowsPT - 1) / kRowsPT);
+    const int grid = tiles < sms * kInferCtas ? tiles : sms * kInferCtas;
+    k<<<grid, kRowsPT, smem, st>>>(p);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_learned(const LearnedParams& p, bool dbl, cudaStream_t st) {
     cudaError_t e;
     const int sms = sm_count(&e);
     if (e != cudaSuccess)
         return e;
-    const long long tiles = (long long)p.a.s.rows * ((p.a.s.cols + kRowsPT - 1) / kRowsPT);
-    const int grid = (int)(tiles < (long long)sms * kInferCtas ? tiles : (long long)sms * kInferCtas);
-    if (p.a.s.elem_bytes == 1) {
-        if (dbl)
-            k_learned<uint8_t, true><<<grid, kRowsPT, 0, st>>>(p);
-        else
-            k_learned<uint8_t, false><<<grid, kRowsPT, 0, st>>>(p);
-    } else {
-        if (dbl)
-            k_learned<uint16_t, true><<<grid, kRowsPT, 0, st>>>(p);
-        else
-            k_learned<uint16_t, false><<<grid, kRowsPT, 0, st>>>(p);
-    }
-    return cudaGetLastError();
+    if (p.a.s.elem_bytes == 1)
+        return dbl ? launch_learned_t<uint8_t, true>(p, sms, st) : launch_learned_t<uint8_t, false>(p, sms, st);
+    return dbl ? launch_learned_t<uint16_t, true>(p, sms, st) : launch_learned_t<uint16_t, false>(p, sms, st);
 }
 
 unsigned int read_mlp_faults() {

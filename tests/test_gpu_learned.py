@@ -166,6 +166,22 @@ def test_check_and_fallback_vs_oracle(cuda, oracle, committed_model, bits, n, do
     _check_case(cuda, oracle, sc, 0.9 if mv else 0.5, 0.1, mv, double, full=(bits == 12 and n <= 16))
 
 
+@pytest.mark.parametrize("cols", [640, 600])
+def test_check_wide_disparity_spread(cuda, oracle, committed_model, cols):
+    """tiles whose matches spread past the staged window read the frames from
+    global memory; rows of 640 (16-byte loads) and 600 columns (element
+    loads)"""
+    sc = scenes.make_scene(24, cols, 16, seed=31, d_range=(5.0, 200.0))
+    _check_case(cuda, oracle, sc, 0.5, 0.1, None, False)
+
+
+@pytest.mark.parametrize("step", [0.05, 0.5])
+def test_fallback_sweep_steps(cuda, oracle, random_model, step):
+    """the warp-per-pixel fallback sweep for other steps (41 and 5 offsets)"""
+    sc = scenes.make_scene(32, 320, 12, seed=13)
+    _check_case(cuda, oracle, sc, 0.5, step, 1.0, True)
+
+
 @pytest.mark.parametrize("double", [False, True])
 def test_fallback_list_with_untrained_model(cuda, oracle, random_model, double):
     sc = scenes.make_scene(48, 400, 16, seed=11)
