@@ -258,6 +258,57 @@ bicos_status bicos_mlp_propose_v1(const float* model, const float* features, int
                                   void* stream);
 
 /*
+ * Batch API (extension; the reference matches one stack per call).
+ *
+ * A handle owns device workspaces, captured CUDA graphs and a tuning table;
+ * it serves one device and one thread at a time.  bicos_match_batch_v1
+ * matches `count` items -- each a bicos_match_v1 argument set, stacks of any
+ * size, depth, input type and configuration -- in one CUDA graph on
+ * `stream`: persistent multi-stack launches for the descriptor transform and
+ * the reference-form agreement, the Hamming search per stack on concurrent
+ * graph branches.  The graph is captured on the first call with a given
+ * signature (shapes, types, configurations, buffer addresses, tuning) and
+ * replayed by later calls; each item's results are bit-identical to
+ * bicos_match_v1 on the same arguments.  Validation errors name the item
+ * ("batch item 3: ...") and launch nothing.  Replays of one graph are
+ * ordered on the streams they are issued to.
+ *
+ * bicos_batch_autotune_v1 times graph replays over the launch shapes
+ * (transform block width, persistent CTAs per SM, virtual blocks per claim,
+ * search branches), keeps the fastest for batches of this shape signature
+ * (addresses aside) and returns it; results do not depend on the tuning.
+ * bicos_batch_set_tuning_v1 fixes a tuning (NULL restores the default and
+ * the tuned table); bicos_batch_captures counts graph captures.
+ */
+typedef struct bicos_batch bicos_batch;
+
+typedef struct bicos_batch_item {
+    const bicos_image* stack0;
+    const bicos_image* stack1;
+    uint32_t n;
+    bicos_image* disparity;
+    bicos_image* corrmap; /* nullable */
+    const bicos_config* cfg;
+} bicos_batch_item;
+
+typedef struct bicos_batch_tuning {
+    int32_t transform_block; /* 64, 128, 256 or 512 threads (default 256) */
+    int32_t ctas_per_sm;     /* persistent launches: CTAs per SM, 1..32 (default 8) */
+    int32_t claim;           /* virtual blocks a CTA claims at a time, 1..64 (default 2) */
+    int32_t branches;        /* concurrent branches of the per-stack search, 1..4 (default 4) */
+} bicos_batch_tuning;
+
+bicos_status bicos_batch_create(bicos_batch** out);
+bicos_status bicos_batch_destroy(bicos_batch* batch);
+bicos_status bicos_match_batch_v1(bicos_batch* batch, const bicos_batch_item* items, uint32_t count,
+                                  bicos_stream_t stream);
+bicos_status bicos_batch_autotune_v1(bicos_batch* batch, const bicos_batch_item* items, uint32_t count,
+                                     bicos_stream_t stream, bicos_batch_tuning* chosen);
+bicos_status bicos_batch_get_tuning_v1(const bicos_batch* batch, bicos_batch_tuning* out);
+bicos_status bicos_batch_set_tuning_v1(bicos_batch* batch, const bicos_batch_tuning* tuning);
+int32_t bicos_batch_captures(const bicos_batch* batch);
+
+/*
  * Stage timing for measurement tools (no counterpart in the reference,
  * whose CLI times whole calls with std::chrono, src/cli.cpp:188-194).  While
  * enabled, each bicos_match_v1 call records CUDA events on its stream

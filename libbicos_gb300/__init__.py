@@ -19,7 +19,7 @@ from .pybicos import Config, Precision, TransformMode, Variant
 
 __all__ = ["pybicos", "Config", "Precision", "TransformMode", "Variant", "match_device",
            "descriptor_transform", "search", "agree", "agree_subpixel", "descriptor_words",
-           "subpixel_features", "agree_learned",
+           "subpixel_features", "agree_learned", "Batch",
            "load_library", "required_bits"]
 
 
@@ -179,3 +179,82 @@ def agree_learned(raw, stack0, stack1, threshold: float, step: float, min_var=No
                                            C.byref(pi), C.byref(count), _stream_ptr(stream)))
     (torch.cuda.current_stream(raw.device) if stream is None else stream).synchronize()  # the count is host memory
     return out, corr, prop, int(count.value)
+
+
+class Batch:
+    """Many stacks per call (bicos_match_batch_v1): one CUDA graph per batch
+    signature, persistent multi-stack launches, an autotuner over launch
+    shapes.  Each job is (stack0, stack1, cfg) with CUDA tensors as for
+    match_device; outputs are (disparity, corrmap or None) per job.  Reuse
+    the outputs of one call (``outs``) to replay its graph."""
+
+    def __init__(self):
+        self._lib = N.load()
+        h = C.c_void_p()
+        N.check(self._lib.bicos_batch_create(C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if self._h:
+            self._lib.bicos_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def outputs(jobs):
+        import torch
+        outs = []
+        for stack0, _, cfg in jobs:
+            nc = cfg.native()
+            dt, ct = C.c_int32(), C.c_int32()
+            N.check(N.load().bicos_output_types(C.byref(nc), C.byref(dt), C.byref(ct)))
+            f0 = stack0[0]
+            disp = torch.empty(tuple(f0.shape), dtype=torch.int16 if dt.value == N.BICOS_16S else torch.float32,
+                               device=f0.device)
+            corr = None
+            if ct.value >= 0:
+                corr = torch.empty(tuple(f0.shape), dtype=torch.float64 if ct.value == N.BICOS_64F else torch.float32,
+                                   device=f0.device)
+            outs.append((disp, corr))
+        return outs
+
+    def _items(self, jobs, outs, max_bits):
+        keep, items = [], (N.BatchItem * len(jobs))()
+        for k, ((stack0, stack1, cfg), (disp, corr)) in enumerate(zip(jobs, outs)):
+            a0, n, _ = _frames(stack0)
+            a1, n1, _ = _frames(stack1)
+            if n1 != n:
+                raise pybicos.Exception("both stacks must hold the same number of images")
+            nc = cfg.native()
+            nc.max_bits = max_bits
+            di = N.tensor_image(disp)
+            ci = N.tensor_image(corr) if corr is not None else None
+            keep += [a0, a1, nc, di, ci]
+            items[k] = N.BatchItem(a0, a1, n, C.pointer(di), C.pointer(ci) if ci is not None else None,
+                                   C.pointer(nc))
+        return items, keep
+
+    def match(self, jobs, outs=None, stream=None, max_bits: int = 256):
+        outs = self.outputs(jobs) if outs is None else outs
+        items, keep = self._items(jobs, outs, max_bits)
+        _raise(self._lib.bicos_match_batch_v1(self._h, items, len(jobs), _stream_ptr(stream)))
+        return outs
+
+    def autotune(self, jobs, outs, stream=None, max_bits: int = 256) -> dict:
+        items, keep = self._items(jobs, outs, max_bits)
+        t = N.BatchTuning()
+        _raise(self._lib.bicos_batch_autotune_v1(self._h, items, len(jobs), _stream_ptr(stream), C.byref(t)))
+        return {f: getattr(t, f) for f, _ in N.BatchTuning._fields_}
+
+    def set_tuning(self, tuning: dict | None):
+        t = None if tuning is None else N.BatchTuning(**tuning)
+        _raise(self._lib.bicos_batch_set_tuning_v1(self._h, C.byref(t) if t is not None else None))
+
+    @property
+    def captures(self) -> int:
+        return self._lib.bicos_batch_captures(self._h)

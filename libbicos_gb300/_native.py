@@ -35,6 +35,16 @@ class Config(C.Structure):
     ]
 
 
+class BatchItem(C.Structure):
+    _fields_ = [("stack0", C.POINTER(Image)), ("stack1", C.POINTER(Image)), ("n", C.c_uint32),
+                ("disparity", C.POINTER(Image)), ("corrmap", C.POINTER(Image)), ("cfg", C.POINTER(Config))]
+
+
+class BatchTuning(C.Structure):
+    _fields_ = [("transform_block", C.c_int32), ("ctas_per_sm", C.c_int32), ("claim", C.c_int32),
+                ("branches", C.c_int32)]
+
+
 class NativeError(Exception):
     """A non-OK bicos_status with the library's message."""
 
@@ -88,6 +98,13 @@ def load():
         "bicos_mlp_grad_v1": ([P, P, C.c_int, P, P, P], C.c_int),
         "bicos_mlp_adam_v1": ([P, P, P, P, C.c_int, F, F, P], C.c_int),
         "bicos_mlp_propose_v1": ([P, P, C.c_int, P, P], C.c_int),
+        "bicos_batch_create": ([C.POINTER(P)], C.c_int),
+        "bicos_batch_destroy": ([P], C.c_int),
+        "bicos_match_batch_v1": ([P, C.POINTER(BatchItem), U, P], C.c_int),
+        "bicos_batch_autotune_v1": ([P, C.POINTER(BatchItem), U, P, C.POINTER(BatchTuning)], C.c_int),
+        "bicos_batch_get_tuning_v1": ([P, C.POINTER(BatchTuning)], C.c_int),
+        "bicos_batch_set_tuning_v1": ([P, C.POINTER(BatchTuning)], C.c_int),
+        "bicos_batch_captures": ([P], I),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

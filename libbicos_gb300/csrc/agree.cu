@@ -16,6 +16,7 @@
 
 #include <type_traits>
 
+#include "batch.cuh"
 #include "kernels.cuh"
 #include "ncc.cuh"
 
@@ -123,11 +124,13 @@ __device__ __forceinline__ typename Prec<DBL>::T nxc_full(const int (&x)[NMAX], 
 }
 
 // agree, in place on the int16 disparity (agree.hpp:52-92, agree.cuh:110-159)
+// Block bodies take the block coordinates as arguments, so the same code
+// runs as a grid over one stack and inside a persistent multi-stack launch
+// (batch.cuh): bx = column block, row.
 template<typename T, bool DBL, int NMAX>
-__global__ void __launch_bounds__(128) k_agree(const __grid_constant__ AgreeParams p) {
+__device__ __forceinline__ void agree_block_body(const AgreeParams& p, int bx, int row) {
     using TP = typename Prec<DBL>::T;
-    const int col = blockIdx.x * blockDim.x + threadIdx.x;
-    const int row = blockIdx.y;
+    const int col = bx * blockDim.x + threadIdx.x;
     const int cols = p.s.cols, n = p.s.n;
     if (col >= cols)
         return;
@@ -153,6 +156,11 @@ __global__ void __launch_bounds__(128) k_agree(const __grid_constant__ AgreePara
     put_corr<TP>(p, row, col, nxc);
     if (nxc < (TP)p.thr)
         *dp = kInvalidDisp;
+}
+
+template<typename T, bool DBL, int NMAX>
+__global__ void __launch_bounds__(128) k_agree(const __grid_constant__ AgreeParams p) {
+    agree_block_body<T, DBL, NMAX>(p, blockIdx.x, blockIdx.y);
 }
 
 constexpr int kListThreads = 128;
@@ -305,12 +313,11 @@ __device__ __forceinline__ float nxc_from(float cov, float var0, float var1, boo
 }
 
 template<typename T, int NMAX>
-__global__ void __launch_bounds__(kSubThreads) k_subpixel_f32(const __grid_constant__ AgreeParams p) {
+__device__ __forceinline__ void subpixel_f32_body(const AgreeParams& p, int bx, int row) {
     constexpr int XG = NMAX <= 33 ? 4 : 2;
     extern __shared__ float4 coef[];  // [NMAX][kSubThreads]: a, b, c, d0
     const int tid = threadIdx.x;
-    const int col = blockIdx.x * kSubThreads + tid;
-    const int row = blockIdx.y;
+    const int col = bx * kSubThreads + tid;
     const int cols = p.s.cols, n = p.s.n;
     if (col >= cols)
         return;
@@ -422,6 +429,11 @@ __global__ void __launch_bounds__(kSubThreads) k_subpixel_f32(const __grid_const
     put_corr<float>(p, row, col, corr);
 }
 
+template<typename T, int NMAX>
+__global__ void __launch_bounds__(kSubThreads) k_subpixel_f32(const __grid_constant__ AgreeParams p) {
+    subpixel_f32_body<T, NMAX>(p, blockIdx.x, blockIdx.y);
+}
+
 // Double-precision subpixel sweep (the reference's nxcorrd,
 // include/impl/cuda/agree.cuh:35-65, in agree.cuh:161-259),
 // with FP64 work only where it can decide the result:
@@ -473,12 +485,11 @@ __device__ double nxcorrd_at(const float4* coef, int tid, int n, double m0, doub
 }
 
 template<typename T, int NMAX>
-__global__ void __launch_bounds__(kSubThreads) k_subpixel_f64(const __grid_constant__ AgreeParams p) {
+__device__ __forceinline__ void subpixel_f64_body(const AgreeParams& p, int bx, int row) {
     using Acc = typename std::conditional<sizeof(T) == 1, int, long long>::type;
     extern __shared__ float4 coef[];  // [NMAX][kSubThreads]: a, b, c, left sample (int bits)
     const int tid = threadIdx.x;
-    const int col = blockIdx.x * kSubThreads + tid;
-    const int row = blockIdx.y;
+    const int col = bx * kSubThreads + tid;
     const int cols = p.s.cols, n = p.s.n;
     if (col >= cols)
         return;
@@ -623,6 +634,46 @@ __global__ void __launch_bounds__(kSubThreads) k_subpixel_f64(const __grid_const
     put_corr<double>(p, row, col, corr);
 }
 
+template<typename T, int NMAX>
+__global__ void __launch_bounds__(kSubThreads) k_subpixel_f64(const __grid_constant__ AgreeParams p) {
+    subpixel_f64_body<T, NMAX>(p, blockIdx.x, blockIdx.y);
+}
+
+// persistent multi-stack forms (batch.cuh)
+template<typename T, bool DBL, int NMAX>
+struct AgreeOp {
+    using P = AgreeParams;
+    static constexpr int kMaxThreads = 128;
+    static __device__ __forceinline__ void run(const P& p, int bx, int row, int) {
+        agree_block_body<T, DBL, NMAX>(p, bx, row);
+    }
+};
+template<typename T, int NMAX>
+struct SubF32Op {
+    using P = AgreeParams;
+    static constexpr int kMaxThreads = kSubThreads;
+    static __device__ __forceinline__ void run(const P& p, int bx, int row, int) {
+        subpixel_f32_body<T, NMAX>(p, bx, row);
+    }
+};
+template<typename T, int NMAX>
+struct SubF64Op {
+    using P = AgreeParams;
+    static constexpr int kMaxThreads = kSubThreads;
+    static __device__ __forceinline__ void run(const P& p, int bx, int row, int) {
+        subpixel_f64_body<T, NMAX>(p, bx, row);
+    }
+};
+
+// the sweep's offsets: -1, then float additions of the step while <= 1
+__global__ void k_sweep_offsets(float step, float* __restrict__ xs, int nx) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        int k = 0;
+        for (float x = -1.f; x <= 1.f && k < nx; x = __fadd_rn(x, step))
+            xs[k++] = x;
+    }
+}
+
 template<typename T, int NM>
 cudaError_t launch_subpixel_f64(const AgreeParams& p, cudaStream_t st) {
     const size_t smem = (size_t)NM * kSubThreads * sizeof(float4);
@@ -704,6 +755,62 @@ cudaError_t launch_subpixel_list(const AgreeParams& p, bool dbl, const int* list
                    : launch_list_t<uint8_t, false>(p, list, count, xs, nx, st);
     return dbl ? launch_list_t<uint16_t, true>(p, list, count, xs, nx, st)
                : launch_list_t<uint16_t, false>(p, list, count, xs, nx, st);
+}
+
+namespace {
+template<typename T, int NM>
+cudaError_t agree_batch_nm(int kind, bool dbl, const AgreeParams* jobs, const BatchWork& w, const BatchLaunch& l,
+                           cudaStream_t st) {
+    if (kind == 1)
+        return launch_batch_op<SubF32Op<T, NM>>(jobs, w, l, agree_smem(1, NM), st);
+    if (kind == 2)
+        return launch_batch_op<SubF64Op<T, NM>>(jobs, w, l, agree_smem(2, NM), st);
+    return dbl ? launch_batch_op<AgreeOp<T, true, NM>>(jobs, w, l, 0, st)
+               : launch_batch_op<AgreeOp<T, false, NM>>(jobs, w, l, 0, st);
+}
+
+template<typename T>
+cudaError_t agree_batch_t(int kind, bool dbl, int nmax, const AgreeParams* jobs, const BatchWork& w,
+                          const BatchLaunch& l, cudaStream_t st) {
+    switch (nmax) {
+        case 8: return agree_batch_nm<T, 8>(kind, dbl, jobs, w, l, st);
+        case 16: return agree_batch_nm<T, 16>(kind, dbl, jobs, w, l, st);
+        case 24: return agree_batch_nm<T, 24>(kind, dbl, jobs, w, l, st);
+        case 33: return agree_batch_nm<T, 33>(kind, dbl, jobs, w, l, st);
+        case 48: return agree_batch_nm<T, 48>(kind, dbl, jobs, w, l, st);
+        case 65: return agree_batch_nm<T, 65>(kind, dbl, jobs, w, l, st);
+        default: return cudaErrorInvalidValue;
+    }
+}
+}  // namespace
+
+int agree_bucket(int n) {
+    for (int b : {8, 16, 24, 33, 48, 65})
+        if (n <= b)
+            return b;
+    return -1;
+}
+
+int agree_block(int kind) { return kind == 0 ? 128 : kSubThreads; }
+
+size_t agree_smem(int kind, int nmax) { return kind == 0 ? 0 : (size_t)nmax * kSubThreads * sizeof(float4); }
+
+cudaError_t launch_agree_batch(int elem_bytes, int kind, bool dbl, int nmax, const AgreeParams* jobs,
+                               const BatchWork& w, const BatchLaunch& l, cudaStream_t st) {
+    return elem_bytes == 1 ? agree_batch_t<uint8_t>(kind, dbl, nmax, jobs, w, l, st)
+                           : agree_batch_t<uint16_t>(kind, dbl, nmax, jobs, w, l, st);
+}
+
+int sweep_offset_count(float step) {
+    int k = 0;
+    for (float x = -1.f; x <= 1.f; x += step)
+        ++k;
+    return k;
+}
+
+cudaError_t launch_sweep_offsets(float step, float* xs, int nx, cudaStream_t st) {
+    k_sweep_offsets<<<1, 32, 0, st>>>(step, xs, nx);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_agree(const AgreeParams& p, bool dbl, cudaStream_t st) {

@@ -17,6 +17,7 @@
 
 #include "../../include/bicos_c.h"
 #include "kernels.cuh"
+#include "match_plan.hpp"
 
 using namespace bicos_gb300;
 
@@ -201,15 +202,6 @@ struct DeviceGuard {
 // the learned form accepts a proposal when rho(x) >= rho(0) - kLearnedDrop
 constexpr float kLearnedDrop = 0.002f;
 
-// the sweep's offsets: -1, then float-accumulated steps while <= 1
-// (agree.hpp:142-143; the same sequence on every IEEE host)
-std::vector<float> sweep_offsets(float step) {
-    std::vector<float> xs;
-    for (float x = -1.f; x <= 1.f; x += step)
-        xs.push_back(x);
-    return xs;
-}
-
 // scratch of the learned form: the fallback list (one int per pixel), its
 // length, the sweep's offsets (step >= 1e-4: at most 20001 of them)
 constexpr size_t kMaxOffsets = 20480;
@@ -239,10 +231,10 @@ cudaError_t learned_subpixel(const AgreeParams& ap, bool dbl, const float* model
     int* list = reinterpret_cast<int*>(b);
     int* count = reinterpret_cast<int*>(b + align_up(px * 4, 256));
     float* xs = reinterpret_cast<float*>(b + align_up(px * 4, 256) + 256);
-    const std::vector<float> offsets = sweep_offsets(ap.step);
-    if (offsets.size() > kMaxOffsets)
+    const int nx = sweep_offset_count(ap.step);
+    if (nx > (int)kMaxOffsets)
         return cudaErrorInvalidValue;
-    cudaError_t e = cudaMemcpyAsync(xs, offsets.data(), offsets.size() * 4, cudaMemcpyHostToDevice, st);
+    cudaError_t e = launch_sweep_offsets(ap.step, xs, nx, st);
     if (e == cudaSuccess)
         e = cudaMemsetAsync(count, 0, 2 * sizeof(int), st);  // list length and tile counter
     if (e == cudaSuccess) {
@@ -260,7 +252,7 @@ cudaError_t learned_subpixel(const AgreeParams& ap, bool dbl, const float* model
         e = launch_learned(lp, dbl, st);
     }
     if (e == cudaSuccess)
-        e = launch_subpixel_list(ap, dbl, list, count, xs, (int)offsets.size(), st);
+        e = launch_subpixel_list(ap, dbl, list, count, xs, nx, st);
     if (e == cudaSuccess && fallback_count_out)
         e = cudaMemcpyAsync(fallback_count_out, count, sizeof(int), cudaMemcpyDeviceToHost, st);
     return e;
@@ -269,6 +261,135 @@ cudaError_t learned_subpixel(const AgreeParams& ap, bool dbl, const float* model
 }  // namespace
 
 void bicos_gb300::set_last_error(const std::string& msg) { g_last_error = msg; }
+
+// ---- one match: validation, scratch layout, stages (also used by the batch API)
+
+size_t MatchPlan::scratch_bytes() const {
+    return 2 * desc_bytes + raw_bytes + 2 * best_bytes + learned_bytes;
+}
+
+bicos_status bicos_gb300::plan_match(const bicos_image* stack0, const bicos_image* stack1, uint32_t n,
+                                     bicos_image* disparity, bicos_image* corrmap, const bicos_config* cfg,
+                                     MatchPlan* plan) {
+    if (!cfg)
+        return fail(BICOS_ERR_INVALID_ARGUMENT, "null config");
+    int eb = 0;
+    if (bicos_status s = check_stacks(stack0, stack1, n, &eb))
+        return s;
+    MatchPlan& P = *plan;
+    P = MatchPlan{};
+    P.cfg = cfg;
+    P.full = cfg->mode == BICOS_MODE_FULL;
+    const int bits = required_bits((int)n, P.full);
+    P.nw = n <= (uint32_t)kMaxFrames ? words_for((int)n, P.full, cfg->max_bits) : -1;
+    if (P.nw < 0)
+        return fail(BICOS_ERR_INVALID_ARGUMENT,
+                    "input stacks too large, would require " + std::to_string(bits) + " bits");
+    P.rows = stack0[0].rows;
+    P.cols = stack0[0].cols;
+    P.n = (int)n;
+    P.eb = eb;
+    P.thr = cfg->has_threshold != 0;
+    P.sub = P.thr && cfg->has_subpixel_step != 0;
+    P.dbl = cfg->precision == BICOS_PRECISION_DOUBLE;
+    if (P.sub && !step_ok(cfg->subpixel_step))
+        return fail(BICOS_ERR_EXCEPTION, "subpixel step must be a finite value >= 1e-4");
+    P.consistency = cfg->variant == BICOS_VARIANT_CONSISTENCY;
+    if (cfg->nxcorr_form < BICOS_NXCORR_REFERENCE || cfg->nxcorr_form > BICOS_NXCORR_LEARNED)
+        return fail(BICOS_ERR_INVALID_ARGUMENT, "unknown nxcorr_form " + std::to_string(cfg->nxcorr_form));
+    if (!image_ok(disparity, P.rows, P.cols, P.sub ? BICOS_32F : BICOS_16S))
+        return fail(BICOS_ERR_EXCEPTION, P.sub ? "disparity must be a float32 image of the stack's size"
+                                               : "disparity must be an int16 image of the stack's size");
+    if (P.thr && corrmap && !image_ok(corrmap, P.rows, P.cols, P.dbl ? BICOS_64F : BICOS_32F))
+        return fail(BICOS_ERR_EXCEPTION, P.dbl ? "corrmap must be a float64 image of the stack's size"
+                                               : "corrmap must be a float32 image of the stack's size");
+    P.moments = P.thr && cfg->nxcorr_form == BICOS_NXCORR_MOMENTS;
+    P.learned = P.sub && cfg->nxcorr_form == BICOS_NXCORR_LEARNED;
+    P.disparity = disparity;
+    P.corrmap = P.thr ? corrmap : nullptr;
+    fill_stack(P.s, stack0, stack1, n, eb);
+    const size_t px = (size_t)P.rows * P.cols;
+    P.desc_bytes = align_up(px * P.nw * 4, 256);
+    P.raw_bytes = P.sub ? align_up(px * 2, 256) : 0;
+    P.best_bytes = P.consistency ? align_up(px * 4, 256) : 0;
+    P.learned_bytes = P.learned ? learned_scratch_bytes(px) : 0;
+    return BICOS_OK;
+}
+
+MatchBuffers bicos_gb300::match_buffers(const MatchPlan& P, void* scratch) {
+    char* b = static_cast<char*>(scratch);
+    MatchBuffers m;
+    m.d0 = reinterpret_cast<uint32_t*>(b);
+    m.d1 = reinterpret_cast<uint32_t*>(b + P.desc_bytes);
+    m.raw = P.sub ? reinterpret_cast<int16_t*>(b + 2 * P.desc_bytes) : static_cast<int16_t*>(P.disparity->data);
+    m.raw_pitch = P.sub ? (long long)P.cols * 2 : (long long)P.disparity->step;
+    m.fwd = P.consistency ? reinterpret_cast<int32_t*>(b + 2 * P.desc_bytes + P.raw_bytes) : nullptr;
+    m.rev = P.consistency ? reinterpret_cast<int32_t*>(b + 2 * P.desc_bytes + P.raw_bytes + P.best_bytes) : nullptr;
+    m.learned = P.learned ? b + 2 * P.desc_bytes + P.raw_bytes + 2 * P.best_bytes : nullptr;
+    return m;
+}
+
+cudaError_t bicos_gb300::enqueue_transform(const MatchPlan& P, const MatchBuffers& m, cudaStream_t st) {
+    return launch_transform(P.s, 2, P.full, P.nw, m.d0, m.d1, st);
+}
+
+cudaError_t bicos_gb300::enqueue_search(const MatchPlan& P, const MatchBuffers& m, cudaStream_t st) {
+    if (P.consistency) {
+        cudaError_t e = launch_search(m.d0, m.d1, P.rows, P.cols, P.nw, P.cfg->no_dupes != 0, 2, nullptr, 0, m.fwd,
+                                      m.rev, st);
+        if (e == cudaSuccess)
+            e = launch_consistency(m.fwd, m.rev, P.rows, P.cols, P.cfg->max_lr_diff, m.raw, m.raw_pitch, st);
+        return e;
+    }
+    return launch_search(m.d0, m.d1, P.rows, P.cols, P.nw, true, 1, m.raw, m.raw_pitch, nullptr, nullptr, st);
+}
+
+AgreeParams bicos_gb300::agree_params(const MatchPlan& P, const MatchBuffers& m) {
+    AgreeParams ap;
+    std::memset(&ap, 0, sizeof ap);
+    ap.s = P.s;
+    ap.thr = P.cfg->nxcorr_threshold;
+    ap.step = P.sub ? P.cfg->subpixel_step : -1.f;
+    ap.has_minvar = P.cfg->has_min_variance != 0;
+    ap.minvar = P.cfg->has_min_variance ? P.cfg->min_variance * (float)P.n : 0.f;  // src/impl/cpu.cpp:123
+    ap.corr = P.corrmap ? P.corrmap->data : nullptr;
+    ap.corr_pitch = P.corrmap ? (long long)P.corrmap->step : 0;
+    ap.raw = m.raw;
+    ap.raw_pitch = m.raw_pitch;
+    if (P.sub) {
+        ap.out = P.disparity->data;
+        ap.out_pitch = (long long)P.disparity->step;
+    } else {
+        ap.raw_io = m.raw;
+    }
+    return ap;
+}
+
+cudaError_t bicos_gb300::enqueue_agree(const MatchPlan& P, const MatchBuffers& m, const float* model,
+                                       cudaStream_t st) {
+    if (!P.thr)
+        return cudaSuccess;
+    const AgreeParams ap = agree_params(P, m);
+    if (P.moments) {
+        MomentParams mp;
+        std::memset(&mp, 0, sizeof mp);
+        mp.s = ap.s;
+        mp.raw = m.raw;
+        mp.raw_pitch = m.raw_pitch;
+        mp.out = P.sub ? P.disparity->data : m.raw;
+        mp.out_pitch = P.sub ? (long long)P.disparity->step : m.raw_pitch;
+        mp.corr = ap.corr;
+        mp.corr_pitch = ap.corr_pitch;
+        mp.thr = ap.thr;
+        mp.step = ap.step;
+        mp.has_minvar = ap.has_minvar;
+        mp.minvar = ap.minvar;
+        return launch_moments(mp, P.sub ? 1 : 0, P.dbl, st);
+    }
+    if (P.learned)
+        return learned_subpixel(ap, P.dbl, model, m.learned, nullptr, nullptr, 0, st);
+    return P.sub ? launch_agree_subpixel(ap, P.dbl, st) : launch_agree(ap, P.dbl, st);
+}
 
 extern "C" {
 
@@ -359,130 +480,38 @@ bicos_status bicos_release_scratch(void) {
 bicos_status bicos_match_v1(const bicos_image* stack0, const bicos_image* stack1, uint32_t n,
                             bicos_image* disparity, bicos_image* corrmap, const bicos_config* cfg,
                             bicos_stream_t stream) {
-    if (!cfg)
-        return fail(BICOS_ERR_INVALID_ARGUMENT, "null config");
-    int eb = 0;
-    if (bicos_status s = check_stacks(stack0, stack1, n, &eb))
+    MatchPlan plan;
+    if (bicos_status s = plan_match(stack0, stack1, n, disparity, corrmap, cfg, &plan))
         return s;
-    const bool full = cfg->mode == BICOS_MODE_FULL;
-    const int bits = required_bits((int)n, full);
-    const int nw = n <= (uint32_t)kMaxFrames ? words_for((int)n, full, cfg->max_bits) : -1;
-    if (nw < 0)
-        return fail(BICOS_ERR_INVALID_ARGUMENT,
-                    "input stacks too large, would require " + std::to_string(bits) + " bits");
-    const int rows = stack0[0].rows, cols = stack0[0].cols;
-    const bool thr = cfg->has_threshold != 0;
-    const bool sub = thr && cfg->has_subpixel_step != 0;
-    const bool dbl = cfg->precision == BICOS_PRECISION_DOUBLE;
-    if (sub && !step_ok(cfg->subpixel_step))
-        return fail(BICOS_ERR_EXCEPTION, "subpixel step must be a finite value >= 1e-4");
-    const bool consistency = cfg->variant == BICOS_VARIANT_CONSISTENCY;
-    if (cfg->nxcorr_form < BICOS_NXCORR_REFERENCE || cfg->nxcorr_form > BICOS_NXCORR_LEARNED)
-        return fail(BICOS_ERR_INVALID_ARGUMENT, "unknown nxcorr_form " + std::to_string(cfg->nxcorr_form));
-    if (!image_ok(disparity, rows, cols, sub ? BICOS_32F : BICOS_16S))
-        return fail(BICOS_ERR_EXCEPTION, sub ? "disparity must be a float32 image of the stack's size"
-                                             : "disparity must be an int16 image of the stack's size");
-    if (thr && corrmap && !image_ok(corrmap, rows, cols, dbl ? BICOS_64F : BICOS_32F))
-        return fail(BICOS_ERR_EXCEPTION, dbl ? "corrmap must be a float64 image of the stack's size"
-                                             : "corrmap must be a float32 image of the stack's size");
-
     DeviceGuard g;
     if (g.err != cudaSuccess)
         return cuda_fail(g.err, "cudaGetDevice");
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    const bool learned = sub && cfg->nxcorr_form == BICOS_NXCORR_LEARNED;
     const float* model = nullptr;
-    if (learned) {
+    if (plan.learned) {
         std::string err;
         model = learned_model_device(st, &err);
         if (!model)
             return fail(BICOS_ERR_INVALID_ARGUMENT, err);
     }
-
-    // scratch: descriptors of both sides, raw disparity, consistency bests,
-    // the learned form's buffers
-    const size_t px = (size_t)rows * cols;
-    const size_t desc_bytes = align_up(px * nw * 4, 256);
-    const size_t raw_bytes = sub ? align_up(px * 2, 256) : 0;
-    const size_t best_bytes = consistency ? align_up(px * 4, 256) : 0;
-    const size_t learned_bytes = learned ? learned_scratch_bytes(px) : 0;
-    const size_t need = 2 * desc_bytes + raw_bytes + 2 * best_bytes + learned_bytes;
-
     Scratch& s = g_scratch[g.dev % kMaxDevices];
     std::lock_guard<std::mutex> lk(s.mu);
     void* base = nullptr;
-    BICOS_CUDA_TRY(scratch_acquire(s, need, st, &base));
-    char* b = static_cast<char*>(base);
-    uint32_t* d0 = reinterpret_cast<uint32_t*>(b);
-    uint32_t* d1 = reinterpret_cast<uint32_t*>(b + desc_bytes);
-    int16_t* raw = sub ? reinterpret_cast<int16_t*>(b + 2 * desc_bytes) : static_cast<int16_t*>(disparity->data);
-    const long long raw_pitch = sub ? (long long)cols * 2 : (long long)disparity->step;
-    int32_t* fwd = consistency ? reinterpret_cast<int32_t*>(b + 2 * desc_bytes + raw_bytes) : nullptr;
-    int32_t* rev = consistency ? reinterpret_cast<int32_t*>(b + 2 * desc_bytes + raw_bytes + best_bytes) : nullptr;
-
-    AgreeParams ap;
-    std::memset(&ap, 0, sizeof ap);
-    fill_stack(ap.s, stack0, stack1, n, eb);
+    BICOS_CUDA_TRY(scratch_acquire(s, plan.scratch_bytes(), st, &base));
+    const MatchBuffers bufs = match_buffers(plan, base);
 
     cudaEvent_t* tev = timing_slot();
     if (tev)
         cudaEventRecord(tev[0], st);
-    cudaError_t e = launch_transform(ap.s, 2, full, nw, d0, d1, st);
+    cudaError_t e = enqueue_transform(plan, bufs, st);
     if (tev)
         cudaEventRecord(tev[1], st);
-    if (e == cudaSuccess) {
-        if (consistency) {
-            e = launch_search(d0, d1, rows, cols, nw, cfg->no_dupes != 0, 2, nullptr, 0, fwd, rev, st);
-            if (e == cudaSuccess)
-                e = launch_consistency(fwd, rev, rows, cols, cfg->max_lr_diff, raw, raw_pitch, st);
-        } else {
-            e = launch_search(d0, d1, rows, cols, nw, true, 1, raw, raw_pitch, nullptr, nullptr, st);
-        }
-    }
+    if (e == cudaSuccess)
+        e = enqueue_search(plan, bufs, st);
     if (tev)
         cudaEventRecord(tev[2], st);
-    if (e == cudaSuccess && thr) {
-        ap.thr = cfg->nxcorr_threshold;
-        ap.step = sub ? cfg->subpixel_step : -1.f;
-        ap.has_minvar = cfg->has_min_variance != 0;
-        ap.minvar = cfg->has_min_variance ? cfg->min_variance * (float)n : 0.f;  // src/impl/cpu.cpp:123
-        ap.corr = corrmap ? corrmap->data : nullptr;
-        ap.corr_pitch = corrmap ? (long long)corrmap->step : 0;
-        if (cfg->nxcorr_form == BICOS_NXCORR_MOMENTS) {
-            MomentParams mp;
-            std::memset(&mp, 0, sizeof mp);
-            mp.s = ap.s;
-            mp.raw = raw;
-            mp.raw_pitch = raw_pitch;
-            mp.out = sub ? disparity->data : raw;
-            mp.out_pitch = sub ? (long long)disparity->step : raw_pitch;
-            mp.corr = ap.corr;
-            mp.corr_pitch = ap.corr_pitch;
-            mp.thr = ap.thr;
-            mp.step = ap.step;
-            mp.has_minvar = ap.has_minvar;
-            mp.minvar = ap.minvar;
-            e = launch_moments(mp, sub ? 1 : 0, dbl, st);
-        } else if (learned) {
-            ap.raw = raw;
-            ap.raw_pitch = raw_pitch;
-            ap.out = disparity->data;
-            ap.out_pitch = (long long)disparity->step;
-            ap.step = cfg->subpixel_step;
-            e = learned_subpixel(ap, dbl, model, b + 2 * desc_bytes + raw_bytes + 2 * best_bytes, nullptr, nullptr,
-                                 0, st);
-        } else if (sub) {
-            ap.raw = raw;
-            ap.raw_pitch = raw_pitch;
-            ap.out = disparity->data;
-            ap.out_pitch = (long long)disparity->step;
-            e = launch_agree_subpixel(ap, dbl, st);
-        } else {
-            ap.raw_io = raw;
-            ap.raw_pitch = raw_pitch;
-            e = launch_agree(ap, dbl, st);
-        }
-    }
+    if (e == cudaSuccess)
+        e = enqueue_agree(plan, bufs, model, st);
     if (tev)
         cudaEventRecord(tev[3], st);
     cudaError_t er = scratch_release(s, st);

@@ -121,6 +121,32 @@ unsigned int read_mlp_faults();
 // message when none is installed)
 const float* learned_model_device(cudaStream_t st, std::string* err);
 
+// batch API (batch.cu): all jobs of one kernel class in one persistent
+// launch over a work table (batch.cuh: BatchWork, BatchLaunch)
+struct BatchWork;
+struct BatchLaunch;
+struct TransformJob {
+    StackParams s;
+    uint32_t* d0;
+    uint32_t* d1;
+};
+// class key: full ? n : descriptor words; virtual grid per job
+// (ceil(cols / block), rows, 2)
+cudaError_t launch_transform_batch(int elem_bytes, bool full, int key, const TransformJob* jobs,
+                                   const BatchWork& w, const BatchLaunch& l, cudaStream_t st);
+// agreement classes: kind 0 agree (in place, int16), 1 single-precision
+// sweep, 2 double-precision sweep; nmax the frame bucket (agree_bucket(n));
+// virtual grid per job (ceil(cols / agree_block(kind)), rows, 1)
+int agree_bucket(int n);
+int agree_block(int kind);
+size_t agree_smem(int kind, int nmax);
+cudaError_t launch_agree_batch(int elem_bytes, int kind, bool dbl, int nmax, const AgreeParams* jobs,
+                               const BatchWork& w, const BatchLaunch& l, cudaStream_t st);
+// the sweep's offsets generated on the device (the same float additions as
+// the reference's loop); nx from sweep_offset_count
+int sweep_offset_count(float step);
+cudaError_t launch_sweep_offsets(float step, float* xs, int nx, cudaStream_t st);
+
 // sets the per-thread message bicos_last_error() returns (defined in capi.cu)
 void set_last_error(const std::string& msg);
 

@@ -9,6 +9,7 @@
 // registers.  The temporal mean is the reference's float RN(sum / n); the
 // sum is exact in int, and `a < mean` is evaluated as `a < ceil(mean)`,
 // which is the same predicate for integer a.
+#include "batch.cuh"
 #include "kernels.cuh"
 
 namespace bicos_gb300 {
@@ -55,12 +56,13 @@ __host__ __device__ constexpr int words_for_bits(int bits) {
 }
 
 // limited mode: 3 bits per t < n-2 plus a pair-sum bit from t >= 2, 4 tail bits
+// block bodies take the block coordinates as arguments, so the same code
+// runs as a grid over one stack and inside a persistent multi-stack launch
+// (batch.cuh): bx = column block, row, side
 template<typename T, int NW, int NMAX>
-__global__ void __launch_bounds__(256) k_transform_limited(const __grid_constant__ StackParams p,
-                                                           uint32_t* __restrict__ d0,
-                                                           uint32_t* __restrict__ d1) {
-    const int col = blockIdx.x * blockDim.x + threadIdx.x;
-    const int row = blockIdx.y, side = blockIdx.z;
+__device__ __forceinline__ void transform_limited(const StackParams& p, uint32_t* __restrict__ d0,
+                                                  uint32_t* __restrict__ d1, int bx, int row, int side) {
+    const int col = bx * blockDim.x + threadIdx.x;
     if (col >= p.cols)
         return;
     const int n = p.n;
@@ -108,16 +110,21 @@ __global__ void __launch_bounds__(256) k_transform_limited(const __grid_constant
     store_desc(((side ? d1 : d0) + ((size_t)row * p.cols + col) * NW), w);
 }
 
+template<typename T, int NW, int NMAX>
+__global__ void __launch_bounds__(256) k_transform_limited(const __grid_constant__ StackParams p,
+                                                           uint32_t* __restrict__ d0,
+                                                           uint32_t* __restrict__ d1) {
+    transform_limited<T, NW, NMAX>(p, d0, d1, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
 // full mode: 3 bits per t < n-2, 3 tail bits, then every ordered pair of
 // non-adjacent pair sums; n is a template parameter so every position is
 // a constant
 template<typename T, int N>
-__global__ void __launch_bounds__(256) k_transform_full(const __grid_constant__ StackParams p,
-                                                        uint32_t* __restrict__ d0,
-                                                        uint32_t* __restrict__ d1) {
+__device__ __forceinline__ void transform_full(const StackParams& p, uint32_t* __restrict__ d0,
+                                               uint32_t* __restrict__ d1, int bx, int row, int side) {
     constexpr int NW = words_for_bits(N * N - 2 * N + 3);
-    const int col = blockIdx.x * blockDim.x + threadIdx.x;
-    const int row = blockIdx.y, side = blockIdx.z;
+    const int col = bx * blockDim.x + threadIdx.x;
     if (col >= p.cols)
         return;
 
@@ -161,6 +168,31 @@ __global__ void __launch_bounds__(256) k_transform_full(const __grid_constant__ 
 
     store_desc(((side ? d1 : d0) + ((size_t)row * p.cols + col) * NW), w);
 }
+
+template<typename T, int N>
+__global__ void __launch_bounds__(256) k_transform_full(const __grid_constant__ StackParams p,
+                                                        uint32_t* __restrict__ d0,
+                                                        uint32_t* __restrict__ d1) {
+    transform_full<T, N>(p, d0, d1, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+// persistent multi-stack forms (batch.cuh)
+template<typename T, int NW, int NMAX>
+struct TfLimitedOp {
+    using P = TransformJob;
+    static constexpr int kMaxThreads = 512;
+    static __device__ __forceinline__ void run(const P& q, int bx, int row, int side) {
+        transform_limited<T, NW, NMAX>(q.s, q.d0, q.d1, bx, row, side);
+    }
+};
+template<typename T, int N>
+struct TfFullOp {
+    using P = TransformJob;
+    static constexpr int kMaxThreads = 512;
+    static __device__ __forceinline__ void run(const P& q, int bx, int row, int side) {
+        transform_full<T, N>(q.s, q.d0, q.d1, bx, row, side);
+    }
+};
 
 template<typename T>
 using tf_kernel_t = void (*)(StackParams, uint32_t*, uint32_t*);
@@ -212,6 +244,40 @@ cudaError_t launch_transform(const StackParams& p, int sides, bool full, int nwo
     const dim3 grid((p.cols + 255) / 256, p.rows, sides);
     k<<<grid, block, 0, st>>>(p, desc0, desc1);
     return cudaGetLastError();
+}
+
+namespace {
+template<typename T>
+cudaError_t transform_batch_t(bool full, int key, const TransformJob* jobs, const BatchWork& w,
+                              const BatchLaunch& l, cudaStream_t st) {
+    if (full) {
+        switch (key) {
+#define BICOS_FULL_CASE(N) \
+    case N: return launch_batch_op<TfFullOp<T, N>>(jobs, w, l, 0, st);
+            BICOS_FULL_CASE(2) BICOS_FULL_CASE(3) BICOS_FULL_CASE(4) BICOS_FULL_CASE(5)
+            BICOS_FULL_CASE(6) BICOS_FULL_CASE(7) BICOS_FULL_CASE(8) BICOS_FULL_CASE(9)
+            BICOS_FULL_CASE(10) BICOS_FULL_CASE(11) BICOS_FULL_CASE(12) BICOS_FULL_CASE(13)
+            BICOS_FULL_CASE(14) BICOS_FULL_CASE(15) BICOS_FULL_CASE(16) BICOS_FULL_CASE(17)
+            BICOS_FULL_CASE(18) BICOS_FULL_CASE(19) BICOS_FULL_CASE(20) BICOS_FULL_CASE(21)
+            BICOS_FULL_CASE(22) BICOS_FULL_CASE(23)
+#undef BICOS_FULL_CASE
+            default: return cudaErrorInvalidValue;
+        }
+    }
+    switch (key) {
+        case 1: return launch_batch_op<TfLimitedOp<T, 1, 9>>(jobs, w, l, 0, st);
+        case 2: return launch_batch_op<TfLimitedOp<T, 2, 17>>(jobs, w, l, 0, st);
+        case 4: return launch_batch_op<TfLimitedOp<T, 4, 33>>(jobs, w, l, 0, st);
+        case 8: return launch_batch_op<TfLimitedOp<T, 8, 65>>(jobs, w, l, 0, st);
+        default: return cudaErrorInvalidValue;
+    }
+}
+}  // namespace
+
+cudaError_t launch_transform_batch(int elem_bytes, bool full, int key, const TransformJob* jobs,
+                                   const BatchWork& w, const BatchLaunch& l, cudaStream_t st) {
+    return elem_bytes == 1 ? transform_batch_t<uint8_t>(full, key, jobs, w, l, st)
+                           : transform_batch_t<uint16_t>(full, key, jobs, w, l, st);
 }
 
 }  // namespace bicos_gb300

@@ -110,3 +110,22 @@ def test_errors_before_any_device_work(native):
 
 def test_version(native):
     assert b"sm_103a" in native.load().bicos_version()
+
+
+def test_batch_handle_host_side(native):
+    """handle life cycle and tuning validation need no GPU"""
+    import ctypes as C
+    lib = native.load()
+    h = C.c_void_p()
+    assert lib.bicos_batch_create(C.byref(h)) == native.OK
+    t = native.BatchTuning()
+    assert lib.bicos_batch_get_tuning_v1(h, C.byref(t)) == native.OK
+    assert (t.transform_block, t.ctas_per_sm, t.claim, t.branches) == (256, 8, 2, 4)
+    bad = native.BatchTuning(100, 1, 1, 1)
+    assert lib.bicos_batch_set_tuning_v1(h, C.byref(bad)) == native.ERR_INVALID_ARGUMENT
+    assert b"out of range" in lib.bicos_last_error()
+    good = native.BatchTuning(128, 4, 1, 2)
+    assert lib.bicos_batch_set_tuning_v1(h, C.byref(good)) == native.OK
+    assert lib.bicos_match_batch_v1(h, None, 0, None) == native.OK  # empty batch: nothing to do
+    assert lib.bicos_batch_captures(h) == 0
+    assert lib.bicos_batch_destroy(h) == native.OK
