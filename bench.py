@@ -51,6 +51,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-double", action="store_true")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned subpixel form")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 16-stack batch comparison")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target CPU work of the baseline sample")
     return ap.parse_args()
 
@@ -210,6 +211,63 @@ def stage_rooflines(stages, rows, cols, n, clk):
     }
 
 
+def batch_bench(lbg, pybicos, scenes, seed, rounds=3, specs=None):
+    """Stacks of mixed size, depth, input type, mode and step (default: the
+    16-stack workload): one bicos_match_batch_v1 graph replay (autotuned
+    launch shapes) against one bicos_match_v1 call per stack, same GPU,
+    same outputs (checked bit for bit)."""
+    import torch
+    specs = scenes.batch_specs(16, seed) if specs is None else specs
+    jobs, px = [], 0
+    for k, (rows, cols, n, bits, full, step) in enumerate(specs):
+        left, right = scenes.make_scene_device(rows, cols, n, seed=seed * 100 + k, bits=bits, d_range=(20.0, 120.0))
+        c = pybicos.Config()
+        c.nxcorr_threshold, c.min_variance, c.subpixel_step = 0.9, 2.0, step
+        c.mode = pybicos.Full if full else pybicos.Limited
+        jobs.append((left, right, c))
+        px += rows * cols
+    stream = torch.cuda.current_stream()
+    seq_outs = lbg.Batch.outputs(jobs)
+
+    def sequential():
+        for (l, r, c), out in zip(jobs, seq_outs):
+            lbg.match_device(l, r, c, out=out)
+
+    b = lbg.Batch()
+    outs = b.match(jobs)
+    tuning = b.autotune(jobs, outs)
+    sequential()
+    b.match(jobs, outs)
+
+    def timed(fn):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(rounds):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / rounds
+
+    ms_seq = timed(sequential)
+    ms_batch = timed(lambda: b.match(jobs, outs))
+
+    def bits(t):
+        return t.view(torch.int16 if t.element_size() == 2 else torch.int32 if t.element_size() == 4 else torch.int64)
+
+    exact = all(torch.equal(bits(a), bits(bb)) and (ca is None or torch.equal(bits(ca), bits(cb)))
+                for (a, ca), (bb, cb) in zip(outs, seq_outs))
+    return {"stacks": len(jobs), "megapixels": round(px / 1e6, 3),
+            "specs": [f"{c}x{r} n={n} {'u16(12-bit)' if bits_ == 12 else 'u8'} {'full' if full else 'limited'} "
+                      f"step={step}" for r, c, n, bits_, full, step in specs],
+            "batched": {"value": round(px / (ms_batch * 1e-3) / 1e6, 3), "unit": "Mpx/s", "ms": round(ms_batch, 3)},
+            "sequential": {"value": round(px / (ms_seq * 1e-3) / 1e6, 3), "unit": "Mpx/s", "ms": round(ms_seq, 3)},
+            "batched_vs_sequential": round(ms_seq / ms_batch, 3), "bit_exact": bool(exact), "tuning": tuning,
+            "graph_captures": b.captures,
+            "data": "seeded synthetic stacks generated on the GPU (make_scene_device), threshold 0.9, "
+                    "min_variance 2.0"}
+
+
 def learned_error(lbg, pybicos, left, right, plain, learned, n):
     """RMS subpixel error (px) of the learned form and of the plain step-0.1
     sweep against the reference sweep with step 0.01 in double precision,
@@ -352,6 +410,16 @@ def run_ours(args):
             "agree_stage_vs_plain_sweep": round(stages[2] / st_l[2], 3),
             "gpu_launches_per_step": 6,
             "error": learned_error(lbg, pybicos, left, right, out[0], out_l[0], n)}
+
+    if not args.no_batch and ws == 1:
+        result["batch"] = batch_bench(lbg, pybicos, scenes, args.seed)
+        # many small stacks, where per-call overhead and kernel tails dominate
+        rng = np.random.default_rng(args.seed + 7)
+        small = [(240, 320, int(rng.choice([8, 12])), 8, bool(rng.random() < 0.5), 0.1 if rng.random() < 0.5 else None)
+                 for _ in range(64)]
+        sm = batch_bench(lbg, pybicos, scenes, args.seed, rounds=10, specs=small)
+        sm.pop("specs")
+        result["batch_small_stacks"] = dict(sm, workload="64 stacks 320x240 u8, n in {8, 12}, mixed mode and step")
 
     if not args.no_e2e:
         # host path: pinned host stacks -> bicos_match_host_v1 (upload, match, download)

@@ -274,8 +274,9 @@ bicos_status bicos_mlp_propose_v1(const float* model, const float* features, int
  * ordered on the streams they are issued to.
  *
  * bicos_batch_autotune_v1 times graph replays over the launch shapes
- * (transform block width, persistent CTAs per SM, virtual blocks per claim,
- * search branches), keeps the fastest for batches of this shape signature
+ * (persistent or per-stack launches per stage, transform block width,
+ * persistent CTAs per SM, virtual blocks per claim, branches), keeps the
+ * fastest for batches of this shape signature
  * (addresses aside) and returns it; results do not depend on the tuning.
  * bicos_batch_set_tuning_v1 fixes a tuning (NULL restores the default and
  * the tuned table); bicos_batch_captures counts graph captures.
@@ -292,10 +293,13 @@ typedef struct bicos_batch_item {
 } bicos_batch_item;
 
 typedef struct bicos_batch_tuning {
-    int32_t transform_block; /* 64, 128, 256 or 512 threads (default 256) */
+    int32_t transform_block; /* 64, 128 or 256 threads (default 256) */
     int32_t ctas_per_sm;     /* persistent launches: CTAs per SM, 1..32 (default 8) */
     int32_t claim;           /* virtual blocks a CTA claims at a time, 1..64 (default 2) */
-    int32_t branches;        /* concurrent branches of the per-stack search, 1..4 (default 4) */
+    int32_t branches;        /* concurrent branches of the per-stack work, 1..4 (default 4) */
+    int32_t persistent;      /* bit 0: transform, bit 1: reference-form agreement as persistent
+                                multi-stack launches, else per-stack launches on the branches
+                                (default 3) */
 } bicos_batch_tuning;
 
 bicos_status bicos_batch_create(bicos_batch** out);

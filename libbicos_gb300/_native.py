@@ -42,7 +42,7 @@ class BatchItem(C.Structure):
 
 class BatchTuning(C.Structure):
     _fields_ = [("transform_block", C.c_int32), ("ctas_per_sm", C.c_int32), ("claim", C.c_int32),
-                ("branches", C.c_int32)]
+                ("branches", C.c_int32), ("persistent", C.c_int32)]
 
 
 class NativeError(Exception):

@@ -644,6 +644,7 @@ template<typename T, bool DBL, int NMAX>
 struct AgreeOp {
     using P = AgreeParams;
     static constexpr int kMaxThreads = 128;
+    static constexpr int kMinBlocks = 1;
     static __device__ __forceinline__ void run(const P& p, int bx, int row, int) {
         agree_block_body<T, DBL, NMAX>(p, bx, row);
     }
@@ -652,6 +653,7 @@ template<typename T, int NMAX>
 struct SubF32Op {
     using P = AgreeParams;
     static constexpr int kMaxThreads = kSubThreads;
+    static constexpr int kMinBlocks = 1;
     static __device__ __forceinline__ void run(const P& p, int bx, int row, int) {
         subpixel_f32_body<T, NMAX>(p, bx, row);
     }
@@ -660,6 +662,7 @@ template<typename T, int NMAX>
 struct SubF64Op {
     using P = AgreeParams;
     static constexpr int kMaxThreads = kSubThreads;
+    static constexpr int kMinBlocks = 1;
     static __device__ __forceinline__ void run(const P& p, int bx, int row, int) {
         subpixel_f64_body<T, NMAX>(p, bx, row);
     }
@@ -759,26 +762,26 @@ cudaError_t launch_subpixel_list(const AgreeParams& p, bool dbl, const int* list
 
 namespace {
 template<typename T, int NM>
-cudaError_t agree_batch_nm(int kind, bool dbl, const AgreeParams* jobs, const BatchWork& w, const BatchLaunch& l,
+cudaError_t agree_batch_nm(int kind, bool dbl, const BatchArgs<AgreeParams>& a, const BatchLaunch& l,
                            cudaStream_t st) {
     if (kind == 1)
-        return launch_batch_op<SubF32Op<T, NM>>(jobs, w, l, agree_smem(1, NM), st);
+        return launch_batch_op<SubF32Op<T, NM>>(a, l, agree_smem(1, NM), st);
     if (kind == 2)
-        return launch_batch_op<SubF64Op<T, NM>>(jobs, w, l, agree_smem(2, NM), st);
-    return dbl ? launch_batch_op<AgreeOp<T, true, NM>>(jobs, w, l, 0, st)
-               : launch_batch_op<AgreeOp<T, false, NM>>(jobs, w, l, 0, st);
+        return launch_batch_op<SubF64Op<T, NM>>(a, l, agree_smem(2, NM), st);
+    return dbl ? launch_batch_op<AgreeOp<T, true, NM>>(a, l, 0, st)
+               : launch_batch_op<AgreeOp<T, false, NM>>(a, l, 0, st);
 }
 
 template<typename T>
-cudaError_t agree_batch_t(int kind, bool dbl, int nmax, const AgreeParams* jobs, const BatchWork& w,
-                          const BatchLaunch& l, cudaStream_t st) {
+cudaError_t agree_batch_t(int kind, bool dbl, int nmax, const BatchArgs<AgreeParams>& a, const BatchLaunch& l,
+                          cudaStream_t st) {
     switch (nmax) {
-        case 8: return agree_batch_nm<T, 8>(kind, dbl, jobs, w, l, st);
-        case 16: return agree_batch_nm<T, 16>(kind, dbl, jobs, w, l, st);
-        case 24: return agree_batch_nm<T, 24>(kind, dbl, jobs, w, l, st);
-        case 33: return agree_batch_nm<T, 33>(kind, dbl, jobs, w, l, st);
-        case 48: return agree_batch_nm<T, 48>(kind, dbl, jobs, w, l, st);
-        case 65: return agree_batch_nm<T, 65>(kind, dbl, jobs, w, l, st);
+        case 8: return agree_batch_nm<T, 8>(kind, dbl, a, l, st);
+        case 16: return agree_batch_nm<T, 16>(kind, dbl, a, l, st);
+        case 24: return agree_batch_nm<T, 24>(kind, dbl, a, l, st);
+        case 33: return agree_batch_nm<T, 33>(kind, dbl, a, l, st);
+        case 48: return agree_batch_nm<T, 48>(kind, dbl, a, l, st);
+        case 65: return agree_batch_nm<T, 65>(kind, dbl, a, l, st);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -795,10 +798,10 @@ int agree_block(int kind) { return kind == 0 ? 128 : kSubThreads; }
 
 size_t agree_smem(int kind, int nmax) { return kind == 0 ? 0 : (size_t)nmax * kSubThreads * sizeof(float4); }
 
-cudaError_t launch_agree_batch(int elem_bytes, int kind, bool dbl, int nmax, const AgreeParams* jobs,
-                               const BatchWork& w, const BatchLaunch& l, cudaStream_t st) {
-    return elem_bytes == 1 ? agree_batch_t<uint8_t>(kind, dbl, nmax, jobs, w, l, st)
-                           : agree_batch_t<uint16_t>(kind, dbl, nmax, jobs, w, l, st);
+cudaError_t launch_agree_batch(int elem_bytes, int kind, bool dbl, int nmax, const BatchArgs<AgreeParams>& a,
+                               const BatchLaunch& l, cudaStream_t st) {
+    return elem_bytes == 1 ? agree_batch_t<uint8_t>(kind, dbl, nmax, a, l, st)
+                           : agree_batch_t<uint16_t>(kind, dbl, nmax, a, l, st);
 }
 
 int sweep_offset_count(float step) {

@@ -44,6 +44,7 @@ struct Tuning {
     int ctas_per_sm = 8;
     int claim = 2;
     int branches = 4;
+    int persistent = 3;  // bit 0: transform, bit 1: agreement as persistent multi-stack launches
 };
 
 struct GraphEntry {
@@ -182,17 +183,9 @@ struct AgClass {
 
 bool batched_agree(const MatchPlan& P) { return P.thr && !P.moments && !P.learned; }
 
-struct Launch {
-    bool transform;
-    TfClass tf;
-    AgClass ag;
-    size_t jobs_off, tiles_off;
-    int nstacks, total, counter;
-    BatchLaunch shape;
-};
-
-// Builds and instantiates the graph of one batch into g (scratch and work
-// tables allocated, tables uploaded before the capture).
+// Builds and instantiates the graph of one batch into g (scratch and claim
+// counters allocated before the capture; the stacks' parameters travel in
+// the persistent launches' kernel parameters).
 cudaError_t build_graph(bicos_batch* b, const std::vector<MatchPlan>& plans, const std::vector<const float*>& models,
                         const Tuning& tn, GraphEntry& g, std::string* where) {
     const size_t count = plans.size();
@@ -210,87 +203,85 @@ cudaError_t build_graph(bicos_batch* b, const std::vector<MatchPlan>& plans, con
     for (size_t i = 0; i < count; ++i)
         bufs[i] = match_buffers(plans[i], static_cast<char*>(g.scratch) + scr_off[i]);
 
-    // work tables
+    // classes, split into launches of at most kBatchJobs stacks
     std::map<TfClass, std::vector<size_t>> tf_classes;
     std::map<AgClass, std::vector<size_t>> ag_classes;
+    const bool tf_persistent = tn.persistent & 1, ag_persistent = tn.persistent & 2;
     for (size_t i = 0; i < count; ++i) {
         const MatchPlan& P = plans[i];
-        tf_classes[{P.eb, P.full, P.full ? P.n : P.nw}].push_back(i);
-        if (batched_agree(P))
+        if (tf_persistent)
+            tf_classes[{P.eb, P.full, P.full ? P.n : P.nw}].push_back(i);
+        if (ag_persistent && batched_agree(P))
             ag_classes[{P.eb, P.sub ? (P.dbl ? 2 : 1) : 0, P.dbl, agree_bucket(P.n)}].push_back(i);
     }
-    std::vector<char> host;
-    std::vector<Launch> launches;
-    auto reserve = [&](size_t bytes) {
-        const size_t off = align256(host.size());
-        host.resize(off + bytes);
-        return off;
-    };
-    int counters = 0;
-    auto claim_grid = [&](int total) {
+    auto grid_of = [&](int total) {
         const int want = (total + tn.claim - 1) / tn.claim;
         return std::max(1, std::min(want, b->sms * tn.ctas_per_sm));
     };
-    for (auto& kv : tf_classes) {
-        Launch L{};
-        L.transform = true;
-        L.tf = kv.first;
-        L.nstacks = (int)kv.second.size();
-        L.jobs_off = reserve(sizeof(TransformJob) * L.nstacks);
-        L.tiles_off = reserve(sizeof(BatchTile) * L.nstacks);
-        int start = 0;
-        for (int j = 0; j < L.nstacks; ++j) {
-            const size_t i = kv.second[j];
-            TransformJob job;
-            job.s = plans[i].s;
-            job.d0 = bufs[i].d0;
-            job.d1 = bufs[i].d1;
-            std::memcpy(host.data() + L.jobs_off + j * sizeof(TransformJob), &job, sizeof job);
-            BatchTile t{start, (plans[i].cols + tn.transform_block - 1) / tn.transform_block, plans[i].rows, 2};
-            std::memcpy(host.data() + L.tiles_off + j * sizeof(BatchTile), &t, sizeof t);
-            start += t.gx * t.gy * t.gz;
+    struct TfLaunch {
+        TfClass c;
+        BatchArgs<TransformJob> a;
+        BatchLaunch l;
+    };
+    struct AgLaunch {
+        AgClass c;
+        BatchArgs<AgreeParams> a;
+        BatchLaunch l;
+    };
+    std::vector<TfLaunch> tf_launches;
+    std::vector<AgLaunch> ag_launches;
+    for (auto& kv : tf_classes)
+        for (size_t c0 = 0; c0 < kv.second.size(); c0 += kBatchJobs) {
+            TfLaunch L;
+            std::memset(&L.a, 0, sizeof L.a);
+            L.c = kv.first;
+            int start = 0, j = 0;
+            for (size_t c = c0; c < std::min(kv.second.size(), c0 + kBatchJobs); ++c, ++j) {
+                const size_t i = kv.second[c];
+                L.a.jobs[j].s = plans[i].s;
+                L.a.jobs[j].d0 = bufs[i].d0;
+                L.a.jobs[j].d1 = bufs[i].d1;
+                L.a.tiles[j] = BatchTile{start, (plans[i].cols + tn.transform_block - 1) / tn.transform_block,
+                                         plans[i].rows, 2};
+                start += L.a.tiles[j].gx * L.a.tiles[j].gy * 2;
+            }
+            L.a.nstacks = j;
+            L.a.total = start;
+            L.a.claim = tn.claim;
+            L.l = BatchLaunch{grid_of(start), tn.transform_block};
+            tf_launches.push_back(L);
         }
-        L.total = start;
-        L.counter = counters++;
-        L.shape = BatchLaunch{claim_grid(start), tn.transform_block};
-        launches.push_back(L);
-    }
-    for (auto& kv : ag_classes) {
-        Launch L{};
-        L.transform = false;
-        L.ag = kv.first;
-        L.nstacks = (int)kv.second.size();
-        L.jobs_off = reserve(sizeof(AgreeParams) * L.nstacks);
-        L.tiles_off = reserve(sizeof(BatchTile) * L.nstacks);
-        const int block = agree_block(L.ag.kind);
-        int start = 0;
-        for (int j = 0; j < L.nstacks; ++j) {
-            const size_t i = kv.second[j];
-            const AgreeParams ap = agree_params(plans[i], bufs[i]);
-            std::memcpy(host.data() + L.jobs_off + j * sizeof(AgreeParams), &ap, sizeof ap);
-            BatchTile t{start, (plans[i].cols + block - 1) / block, plans[i].rows, 1};
-            std::memcpy(host.data() + L.tiles_off + j * sizeof(BatchTile), &t, sizeof t);
-            start += t.gx * t.gy;
+    for (auto& kv : ag_classes)
+        for (size_t c0 = 0; c0 < kv.second.size(); c0 += kBatchJobs) {
+            AgLaunch L;
+            std::memset(&L.a, 0, sizeof L.a);
+            L.c = kv.first;
+            const int block = agree_block(L.c.kind);
+            int start = 0, j = 0;
+            for (size_t c = c0; c < std::min(kv.second.size(), c0 + kBatchJobs); ++c, ++j) {
+                const size_t i = kv.second[c];
+                L.a.jobs[j] = agree_params(plans[i], bufs[i]);
+                L.a.tiles[j] = BatchTile{start, (plans[i].cols + block - 1) / block, plans[i].rows, 1};
+                start += L.a.tiles[j].gx * L.a.tiles[j].gy;
+            }
+            L.a.nstacks = j;
+            L.a.total = start;
+            L.a.claim = tn.claim;
+            L.l = BatchLaunch{grid_of(start), block};
+            ag_launches.push_back(L);
         }
-        L.total = start;
-        L.counter = counters++;
-        L.shape = BatchLaunch{claim_grid(start), block};
-        launches.push_back(L);
-    }
-    const size_t counters_off = reserve(sizeof(int) * std::max(counters, 1));
-    e = cudaMalloc(&g.tables, host.size());
-    if (e == cudaSuccess)
-        e = cudaMemcpy(g.tables, host.data(), host.size(), cudaMemcpyHostToDevice);
+    const int counters = (int)(tf_launches.size() + ag_launches.size());
+    e = cudaMalloc(&g.tables, sizeof(int) * std::max(counters, 1));
     if (e == cudaSuccess)
         e = cudaEventCreateWithFlags(&g.done, cudaEventDisableTiming);
     if (e != cudaSuccess)
         return e;
-    char* dt = static_cast<char*>(g.tables);
-    int* dcounters = reinterpret_cast<int*>(dt + counters_off);
-    auto work = [&](const Launch& L) {
-        return BatchWork{reinterpret_cast<const BatchTile*>(dt + L.tiles_off), L.nstacks, L.total,
-                         dcounters + L.counter, tn.claim};
-    };
+    int* dcounters = static_cast<int*>(g.tables);
+    int next_counter = 0;
+    for (TfLaunch& L : tf_launches)
+        L.a.counter = dcounters + next_counter++;
+    for (AgLaunch& L : ag_launches)
+        L.a.counter = dcounters + next_counter++;
     const int branches = std::max(1, std::min(tn.branches, kMaxBranches));
 
     // capture (a stale error of this thread would be read back by the
@@ -302,13 +293,11 @@ cudaError_t build_graph(bicos_batch* b, const std::vector<MatchPlan>& plans, con
     cudaError_t ce = cudaMemsetAsync(dcounters, 0, sizeof(int) * std::max(counters, 1), b->cap);
     if (ce != cudaSuccess)
         *where = "counter reset";
-    for (const Launch& L : launches)
-        if (ce == cudaSuccess && L.transform) {
-            ce = launch_transform_batch(L.tf.eb, L.tf.full, L.tf.key,
-                                        reinterpret_cast<const TransformJob*>(dt + L.jobs_off), work(L), L.shape,
-                                        b->cap);
+    for (const TfLaunch& L : tf_launches)
+        if (ce == cudaSuccess) {
+            ce = launch_transform_batch(L.c.eb, L.c.full, L.c.key, L.a, L.l, b->cap);
             if (ce != cudaSuccess)
-                *where = "transform launch (key " + std::to_string(L.tf.key) + ")";
+                *where = "transform launch (key " + std::to_string(L.c.key) + ")";
         }
     auto fork_join = [&](int f, auto&& body) {
         cudaError_t r = cudaEventRecord(b->fork[f], b->cap);
@@ -329,29 +318,37 @@ cudaError_t build_graph(bicos_batch* b, const std::vector<MatchPlan>& plans, con
         ce = fork_join(0, [&]() {
             cudaError_t r = cudaSuccess;
             for (size_t i = 0; i < count && r == cudaSuccess; ++i) {
-                r = enqueue_search(plans[i], bufs[i], b->branch[i % branches]);
+                cudaStream_t bs = b->branch[i % branches];
+                if (!tf_persistent) {
+                    r = enqueue_transform(plans[i], bufs[i], bs);
+                    if (r != cudaSuccess) {
+                        *where = "transform of item " + std::to_string(i);
+                        break;
+                    }
+                }
+                r = enqueue_search(plans[i], bufs[i], bs);
                 if (r != cudaSuccess)
                     *where = "search of item " + std::to_string(i);
             }
             return r;
         });
-    for (const Launch& L : launches)
-        if (ce == cudaSuccess && !L.transform) {
-            ce = launch_agree_batch(L.ag.eb, L.ag.kind, L.ag.dbl, L.ag.nmax,
-                                    reinterpret_cast<const AgreeParams*>(dt + L.jobs_off), work(L), L.shape, b->cap);
+    for (const AgLaunch& L : ag_launches)
+        if (ce == cudaSuccess) {
+            ce = launch_agree_batch(L.c.eb, L.c.kind, L.c.dbl, L.c.nmax, L.a, L.l, b->cap);
             if (ce != cudaSuccess)
-                *where = "agreement launch (kind " + std::to_string(L.ag.kind) + ", frames " +
-                         std::to_string(L.ag.nmax) + ")";
+                *where = "agreement launch (kind " + std::to_string(L.c.kind) + ", frames " +
+                         std::to_string(L.c.nmax) + ")";
         }
+    auto per_stack_agree = [&](const MatchPlan& P) { return P.thr && (!ag_persistent || !batched_agree(P)); };
     bool per_stack = false;
     for (const MatchPlan& P : plans)
-        per_stack |= P.thr && !batched_agree(P);
+        per_stack |= per_stack_agree(P);
     if (ce == cudaSuccess && per_stack)
         ce = fork_join(1, [&]() {
             cudaError_t r = cudaSuccess;
             int k = 0;
             for (size_t i = 0; i < count && r == cudaSuccess; ++i)
-                if (plans[i].thr && !batched_agree(plans[i])) {
+                if (per_stack_agree(plans[i])) {
                     r = enqueue_agree(plans[i], bufs[i], models[i], b->branch[k++ % branches]);
                     if (r != cudaSuccess)
                         *where = "agreement of item " + std::to_string(i);
@@ -445,6 +442,7 @@ Tuning from_c(const bicos_batch_tuning& t) {
     r.ctas_per_sm = t.ctas_per_sm;
     r.claim = t.claim;
     r.branches = t.branches;
+    r.persistent = t.persistent;
     return r;
 }
 
@@ -454,14 +452,14 @@ bicos_batch_tuning to_c(const Tuning& t) {
     r.ctas_per_sm = t.ctas_per_sm;
     r.claim = t.claim;
     r.branches = t.branches;
+    r.persistent = t.persistent;
     return r;
 }
 
 bool tuning_ok(const bicos_batch_tuning& t) {
-    return (t.transform_block == 64 || t.transform_block == 128 || t.transform_block == 256 ||
-            t.transform_block == 512) &&
+    return (t.transform_block == 64 || t.transform_block == 128 || t.transform_block == 256) &&
            t.ctas_per_sm >= 1 && t.ctas_per_sm <= 32 && t.claim >= 1 && t.claim <= 64 && t.branches >= 1 &&
-           t.branches <= kMaxBranches;
+           t.branches <= kMaxBranches && t.persistent >= 0 && t.persistent <= 3;
 }
 
 }  // namespace
@@ -559,12 +557,18 @@ bicos_status bicos_batch_autotune_v1(bicos_batch* b, const bicos_batch_item* ite
     Tuning cur = b->tuning;
     float cur_ms = 0.f;
     bicos_status s = measure(cur, &cur_ms);
-    const std::vector<int> blocks = {128, 256, 512}, ctas = {2, 4, 8, 16}, claims = {1, 2, 4}, brs = {1, 2, 4};
-    for (int dim = 0; dim < 4 && s == BICOS_OK; ++dim) {
-        const std::vector<int>& cands = dim == 0 ? blocks : dim == 1 ? ctas : dim == 2 ? claims : brs;
+    const std::vector<int> pers = {0, 1, 2, 3}, blocks = {64, 128, 256}, ctas = {2, 4, 8, 16}, claims = {1, 2, 4},
+                           brs = {1, 2, 4};
+    for (int dim = 0; dim < 5 && s == BICOS_OK; ++dim) {
+        const std::vector<int>& cands =
+            dim == 0 ? pers : dim == 1 ? blocks : dim == 2 ? ctas : dim == 3 ? claims : brs;
         for (int v : cands) {
             Tuning t = cur;
-            int& field = dim == 0 ? t.transform_block : dim == 1 ? t.ctas_per_sm : dim == 2 ? t.claim : t.branches;
+            int& field = dim == 0   ? t.persistent
+                         : dim == 1 ? t.transform_block
+                         : dim == 2 ? t.ctas_per_sm
+                         : dim == 3 ? t.claim
+                                    : t.branches;
             if (field == v)
                 continue;
             field = v;
@@ -616,8 +620,8 @@ bicos_status bicos_batch_set_tuning_v1(bicos_batch* b, const bicos_batch_tuning*
     }
     if (!tuning_ok(*t))
         return batch_fail(BICOS_ERR_INVALID_ARGUMENT,
-                          "batch tuning out of range (transform_block 64/128/256/512, ctas_per_sm 1..32, "
-                          "claim 1..64, branches 1..4)");
+                          "batch tuning out of range (transform_block 64/128/256, ctas_per_sm 1..32, "
+                          "claim 1..64, branches 1..4, persistent 0..3)");
     b->tuning = from_c(*t);
     b->fixed_tuning = true;
     return BICOS_OK;

@@ -123,7 +123,8 @@ const float* learned_model_device(cudaStream_t st, std::string* err);
 
 // batch API (batch.cu): all jobs of one kernel class in one persistent
 // launch over a work table (batch.cuh: BatchWork, BatchLaunch)
-struct BatchWork;
+template<typename P>
+struct BatchArgs;
 struct BatchLaunch;
 struct TransformJob {
     StackParams s;
@@ -132,16 +133,16 @@ struct TransformJob {
 };
 // class key: full ? n : descriptor words; virtual grid per job
 // (ceil(cols / block), rows, 2)
-cudaError_t launch_transform_batch(int elem_bytes, bool full, int key, const TransformJob* jobs,
-                                   const BatchWork& w, const BatchLaunch& l, cudaStream_t st);
+cudaError_t launch_transform_batch(int elem_bytes, bool full, int key, const BatchArgs<TransformJob>& args,
+                                   const BatchLaunch& l, cudaStream_t st);
 // agreement classes: kind 0 agree (in place, int16), 1 single-precision
 // sweep, 2 double-precision sweep; nmax the frame bucket (agree_bucket(n));
 // virtual grid per job (ceil(cols / agree_block(kind)), rows, 1)
 int agree_bucket(int n);
 int agree_block(int kind);
 size_t agree_smem(int kind, int nmax);
-cudaError_t launch_agree_batch(int elem_bytes, int kind, bool dbl, int nmax, const AgreeParams* jobs,
-                               const BatchWork& w, const BatchLaunch& l, cudaStream_t st);
+cudaError_t launch_agree_batch(int elem_bytes, int kind, bool dbl, int nmax, const BatchArgs<AgreeParams>& args,
+                               const BatchLaunch& l, cudaStream_t st);
 // the sweep's offsets generated on the device (the same float additions as
 // the reference's loop); nx from sweep_offset_count
 int sweep_offset_count(float step);

@@ -180,7 +180,8 @@ __global__ void __launch_bounds__(256) k_transform_full(const __grid_constant__ 
 template<typename T, int NW, int NMAX>
 struct TfLimitedOp {
     using P = TransformJob;
-    static constexpr int kMaxThreads = 512;
+    static constexpr int kMaxThreads = 256;
+    static constexpr int kMinBlocks = NW <= 2 ? 8 : NW == 4 ? 4 : 2;
     static __device__ __forceinline__ void run(const P& q, int bx, int row, int side) {
         transform_limited<T, NW, NMAX>(q.s, q.d0, q.d1, bx, row, side);
     }
@@ -188,7 +189,8 @@ struct TfLimitedOp {
 template<typename T, int N>
 struct TfFullOp {
     using P = TransformJob;
-    static constexpr int kMaxThreads = 512;
+    static constexpr int kMaxThreads = 256;
+    static constexpr int kMinBlocks = 4;
     static __device__ __forceinline__ void run(const P& q, int bx, int row, int side) {
         transform_full<T, N>(q.s, q.d0, q.d1, bx, row, side);
     }
@@ -248,12 +250,12 @@ cudaError_t launch_transform(const StackParams& p, int sides, bool full, int nwo
 
 namespace {
 template<typename T>
-cudaError_t transform_batch_t(bool full, int key, const TransformJob* jobs, const BatchWork& w,
-                              const BatchLaunch& l, cudaStream_t st) {
+cudaError_t transform_batch_t(bool full, int key, const BatchArgs<TransformJob>& a, const BatchLaunch& l,
+                              cudaStream_t st) {
     if (full) {
         switch (key) {
 #define BICOS_FULL_CASE(N) \
-    case N: return launch_batch_op<TfFullOp<T, N>>(jobs, w, l, 0, st);
+    case N: return launch_batch_op<TfFullOp<T, N>>(a, l, 0, st);
             BICOS_FULL_CASE(2) BICOS_FULL_CASE(3) BICOS_FULL_CASE(4) BICOS_FULL_CASE(5)
             BICOS_FULL_CASE(6) BICOS_FULL_CASE(7) BICOS_FULL_CASE(8) BICOS_FULL_CASE(9)
             BICOS_FULL_CASE(10) BICOS_FULL_CASE(11) BICOS_FULL_CASE(12) BICOS_FULL_CASE(13)
@@ -265,19 +267,19 @@ cudaError_t transform_batch_t(bool full, int key, const TransformJob* jobs, cons
         }
     }
     switch (key) {
-        case 1: return launch_batch_op<TfLimitedOp<T, 1, 9>>(jobs, w, l, 0, st);
-        case 2: return launch_batch_op<TfLimitedOp<T, 2, 17>>(jobs, w, l, 0, st);
-        case 4: return launch_batch_op<TfLimitedOp<T, 4, 33>>(jobs, w, l, 0, st);
-        case 8: return launch_batch_op<TfLimitedOp<T, 8, 65>>(jobs, w, l, 0, st);
+        case 1: return launch_batch_op<TfLimitedOp<T, 1, 9>>(a, l, 0, st);
+        case 2: return launch_batch_op<TfLimitedOp<T, 2, 17>>(a, l, 0, st);
+        case 4: return launch_batch_op<TfLimitedOp<T, 4, 33>>(a, l, 0, st);
+        case 8: return launch_batch_op<TfLimitedOp<T, 8, 65>>(a, l, 0, st);
         default: return cudaErrorInvalidValue;
     }
 }
 }  // namespace
 
-cudaError_t launch_transform_batch(int elem_bytes, bool full, int key, const TransformJob* jobs,
-                                   const BatchWork& w, const BatchLaunch& l, cudaStream_t st) {
-    return elem_bytes == 1 ? transform_batch_t<uint8_t>(full, key, jobs, w, l, st)
-                           : transform_batch_t<uint16_t>(full, key, jobs, w, l, st);
+cudaError_t launch_transform_batch(int elem_bytes, bool full, int key, const BatchArgs<TransformJob>& a,
+                                   const BatchLaunch& l, cudaStream_t st) {
+    return elem_bytes == 1 ? transform_batch_t<uint8_t>(full, key, a, l, st)
+                           : transform_batch_t<uint16_t>(full, key, a, l, st);
 }
 
 }  // namespace bicos_gb300

@@ -128,3 +128,68 @@ def workload_scene(name: str, seed: int = 0, rows: int | None = None, cols: int 
     if cols is not None:
         kw["cols"] = cols
     return make_scene(seed=seed, **kw)
+
+
+def make_scene_device(rows: int, cols: int, n: int, seed: int = 0, bits: int = 8, d_range=(20.0, 120.0),
+                      sigma=1.5, noise: float | None = None, flat_fraction: float = 0.10, device="cuda"):
+    """The make_scene recipe on the GPU (torch, seeded Philox generator), for
+    stacks too large to synthesise quickly on the host: returns (left, right)
+    as (n, rows, cols) uint8 / uint16 CUDA tensors.  Blur is a separable
+    Gaussian of radius 3 sigma with edge replication."""
+    import torch
+    g = torch.Generator(device=device).manual_seed(seed)
+    rng = np.random.default_rng(seed)
+    scale = 16.0 if bits == 12 else 1.0
+    maxv = 4095 if bits == 12 else 255
+    dtype = torch.int16 if bits > 8 else torch.uint8
+    noise = (8.0 if bits == 12 else 2.0) if noise is None else noise
+    d = torch.from_numpy(disparity_field(rows, cols, rng, *d_range)).to(device=device, dtype=torch.float32)
+    fh, fw = int(rows * np.sqrt(flat_fraction)), int(cols * np.sqrt(flat_fraction))
+    fy = int(rng.integers(0, max(1, rows - fh)))
+    fx = int(rng.integers(0, max(1, cols - fw)))
+    xs = torch.arange(cols, device=device, dtype=torch.float32)[None, :] + d
+    x0 = torch.floor(xs)
+    fr = xs - x0
+    x0c = x0.long().clamp(0, cols - 1)
+    x1c = (x0.long() + 1).clamp(0, cols - 1)
+    r_ = int(3 * sigma + 1)
+    k = torch.exp(-0.5 * (torch.arange(-r_, r_ + 1, device=device, dtype=torch.float32) / sigma) ** 2)
+    k = (k / k.sum()).view(1, 1, -1)
+    left = torch.empty((n, rows, cols), dtype=dtype, device=device)
+    right = torch.empty((n, rows, cols), dtype=dtype, device=device)
+    for t in range(n):
+        z = torch.randn((1, rows, cols), generator=g, device=device)
+        z = torch.nn.functional.conv1d(torch.nn.functional.pad(z.view(rows, 1, cols), (r_, r_), mode="replicate"), k)
+        z = z.view(rows, cols).t().contiguous().view(cols, 1, rows)
+        z = torch.nn.functional.conv1d(torch.nn.functional.pad(z, (r_, r_), mode="replicate"), k).view(cols, rows).t()
+        pat = (z - z.min()) / (z.max() - z.min()).clamp_min(1e-12)
+        img = 125.0 + (pat * 190.0 - 95.0)
+        rimg = torch.gather(img, 1, x0c) * (1 - fr) + torch.gather(img, 1, x1c) * fr
+        rimg = rimg + torch.randn((rows, cols), generator=g, device=device) * (noise / scale)
+        img[fy:fy + fh, fx:fx + fw] = 40.0 + torch.randn((fh, fw), generator=g, device=device) * (noise / scale)
+        rimg[fy:fy + fh, fx:fx + fw] = 40.0 + torch.randn((fh, fw), generator=g, device=device) * (noise / scale)
+        left[t] = torch.round(img * scale).clamp(0, maxv).to(dtype)
+        right[t] = torch.round(rimg * scale).clamp(0, maxv).to(dtype)
+    if bits > 8:  # the matcher takes uint16: same bits
+        left, right = left.view(torch.uint16), right.view(torch.uint16)
+    return left, right
+
+
+# Batching workload: 16 stacks of mixed size, depth, input type, mode and step.
+BATCH_SIZES = [(480, 640), (1024, 1280), (1216, 1936), (2048, 2448)]
+BATCH_DEPTHS = [8, 12, 20, 33, 40]
+
+
+def batch_specs(count: int = 16, seed: int = 0):
+    """(rows, cols, n, bits, full, step) per stack, drawn from seed: FULL
+    descriptors only where the reference allows them (n <= 16)."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    for _ in range(count):
+        rows, cols = BATCH_SIZES[int(rng.integers(len(BATCH_SIZES)))]
+        n = int(rng.choice(BATCH_DEPTHS))
+        bits = 12 if rng.random() < 0.5 else 8
+        full = bool(n <= 16 and rng.random() < 0.5)
+        step = 0.1 if rng.random() < 0.5 else None
+        specs.append((rows, cols, n, bits, full, step))
+    return specs

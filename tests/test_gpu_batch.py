@@ -89,10 +89,11 @@ def test_batch_autotune_and_fixed_tunings(cuda):
     b = lbg.Batch()
     outs = b.match(jobs)
     chosen = b.autotune(jobs, outs)
-    assert chosen["transform_block"] in (128, 256, 512) and chosen["branches"] in (1, 2, 4)
+    assert chosen["transform_block"] in (64, 128, 256) and chosen["branches"] in (1, 2, 4)
     assert_same_as_sequential(jobs, b.match(jobs, outs))
-    for t in ({"transform_block": 64, "ctas_per_sm": 1, "claim": 1, "branches": 1},
-              {"transform_block": 512, "ctas_per_sm": 32, "claim": 64, "branches": 3}):
+    for t in ({"transform_block": 64, "ctas_per_sm": 1, "claim": 1, "branches": 1, "persistent": 3},
+              {"transform_block": 256, "ctas_per_sm": 32, "claim": 64, "branches": 3, "persistent": 1},
+              {"transform_block": 128, "ctas_per_sm": 4, "claim": 2, "branches": 2, "persistent": 0}):
         b.set_tuning(t)
         assert_same_as_sequential(jobs, b.match(jobs, outs))
 
@@ -107,7 +108,7 @@ def test_batch_errors_name_the_item(cuda):
         b.match(bad)
     assert b.captures == 0
     with pytest.raises(ValueError, match="batch tuning out of range"):
-        b.set_tuning({"transform_block": 100, "ctas_per_sm": 1, "claim": 1, "branches": 1})
+        b.set_tuning({"transform_block": 100, "ctas_per_sm": 1, "claim": 1, "branches": 1, "persistent": 3})
 
 
 def test_batch_single_item_and_streams(cuda):

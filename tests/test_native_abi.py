@@ -120,11 +120,11 @@ def test_batch_handle_host_side(native):
     assert lib.bicos_batch_create(C.byref(h)) == native.OK
     t = native.BatchTuning()
     assert lib.bicos_batch_get_tuning_v1(h, C.byref(t)) == native.OK
-    assert (t.transform_block, t.ctas_per_sm, t.claim, t.branches) == (256, 8, 2, 4)
-    bad = native.BatchTuning(100, 1, 1, 1)
+    assert (t.transform_block, t.ctas_per_sm, t.claim, t.branches, t.persistent) == (256, 8, 2, 4, 3)
+    bad = native.BatchTuning(100, 1, 1, 1, 3)
     assert lib.bicos_batch_set_tuning_v1(h, C.byref(bad)) == native.ERR_INVALID_ARGUMENT
     assert b"out of range" in lib.bicos_last_error()
-    good = native.BatchTuning(128, 4, 1, 2)
+    good = native.BatchTuning(128, 4, 1, 2, 1)
     assert lib.bicos_batch_set_tuning_v1(h, C.byref(good)) == native.OK
     assert lib.bicos_match_batch_v1(h, None, 0, None) == native.OK  # empty batch: nothing to do
     assert lib.bicos_batch_captures(h) == 0
