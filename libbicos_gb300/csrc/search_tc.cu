@@ -95,53 +95,44 @@ __device__ __forceinline__ float fmax3(float a, float b, float c) {
     return r;
 }
 
-// top-2 update of (m1, m2) with the pair (a, b).  min/max run on the
-// half-rate ALU pipe, so the pair's minimum is formed as (a + b) - max on
-// the FMA pipe: exact, since keys are multiples of 2^-12 below 2^10 in
-// magnitude.  MASKED pairs may hold -inf and use a plain min instead.
+// Row reduction over the candidates' dot products (dot = bits - 2 *
+// Hamming, integer-valued).  Chain A keeps max(dot - col/4096): the largest
+// dot at its first column, the reference's first minimum.  Chain B (only
+// with no-duplicates) keeps max(dot + col/4096): the same dot at its last
+// column; the minimum cost is duplicated exactly when the two columns
+// differ, which is the reference's no-duplicates rule (a later column with
+// the same cost).  All keys are exact in FP32 (|dot| <= 512, offsets
+// multiples of 2^-12 below 1).  Per pair of candidates: 2 (or 4) FADDs with
+// immediate offsets on the FMA pipe and 1 (or 2) three-input maxima on the
+// ALU pipe.
 template<bool NODUP, bool MASKED>
-__device__ __forceinline__ void top2_pair(float a, float b, float& m1, float& m2) {
-    if constexpr (NODUP) {
-        const float hi = fmaxf(a, b);
-        const float lo = MASKED ? fminf(a, b) : (a + b) - hi;
-        m2 = fmax3(m2, lo, fminf(m1, hi));
-        m1 = fmaxf(m1, hi);
-    } else {
-        m1 = fmax3(m1, a, b);
-    }
-}
-
-// merge top-2 sets (m1, m2) <- (m1, m2) u (r1, r2)
-template<bool NODUP>
-__device__ __forceinline__ void top2_merge(float r1, float r2, float& m1, float& m2) {
-    if constexpr (NODUP)
-        m2 = fmax3(m2, r2, fminf(m1, r1));
-    m1 = fmaxf(m1, r1);
-}
-
-// 32 dot products of columns j0..j0+31 (MASKED: only the first `lim` are
-// real): keys dot - col/4096, four independent chains for ILP
-template<bool NODUP, bool MASKED>
-__device__ __forceinline__ void reduce_chunk(const float (&v)[32], int j0, int lim, float& m1, float& m2) {
-    float c1[4], c2[4];
+__device__ __forceinline__ void reduce_chunk(const float (&v)[32], int j0, int lim, float& mA, float& mB) {
+    float ca[4], cb[4];
 #pragma unroll
     for (int i = 0; i < 4; ++i)
-        c1[i] = c2[i] = -INFINITY;
+        ca[i] = cb[i] = -INFINITY;
 #pragma unroll
     for (int k = 0; k < 32; k += 2) {
-        float a = v[k] - (float)k * kColScale;
-        float b = v[k + 1] - (float)(k + 1) * kColScale;
+        const float va = v[k], vb = v[k + 1];
+        float a = va - (float)k * kColScale;
+        float b = vb - (float)(k + 1) * kColScale;
+        float a2 = va + (float)k * kColScale;
+        float b2 = vb + (float)(k + 1) * kColScale;
         if constexpr (MASKED) {
             a = k < lim ? a : -INFINITY;
             b = k + 1 < lim ? b : -INFINITY;
+            a2 = k < lim ? a2 : -INFINITY;
+            b2 = k + 1 < lim ? b2 : -INFINITY;
         }
-        top2_pair<NODUP, MASKED>(a, b, c1[(k >> 1) & 3], c2[(k >> 1) & 3]);
+        const int i = (k >> 1) & 3;
+        ca[i] = fmax3(ca[i], a, b);
+        if constexpr (NODUP)
+            cb[i] = fmax3(cb[i], a2, b2);
     }
-    top2_merge<NODUP>(c1[1], c2[1], c1[0], c2[0]);
-    top2_merge<NODUP>(c1[3], c2[3], c1[2], c2[2]);
-    top2_merge<NODUP>(c1[2], c2[2], c1[0], c2[0]);
     const float off = (float)j0 * kColScale;
-    top2_merge<NODUP>(c1[0] - off, c2[0] - off, m1, m2);
+    mA = fmax3(mA, fmax3(ca[0], ca[1], ca[2]) - off, ca[3] - off);
+    if constexpr (NODUP)
+        mB = fmax3(mB, fmax3(cb[0], cb[1], cb[2]) + off, cb[3] + off);
 }
 
 // Warp roles of the pipelined CTA (one CTA = one row x 128 query pixels):
@@ -170,7 +161,7 @@ struct TcShared {
     uint64_t acc_empty[2];  // epilogue -> MMA, 256 arrivals
     uint32_t tmem;
     int abort;
-    float2 red[kRows];      // second column half's (m1, m2) per query
+    float2 red[kRows];      // second column half's (chain A, chain B) maxima per query
 };
 
 template<int NW, bool NODUP>
@@ -281,7 +272,7 @@ __global__ void __launch_bounds__(kThreadsTC, 2) k_search_tc(const uint32_t* __r
         // ---- epilogue ----
         const int q = warp & 3, half = warp >> 2;
         const uint32_t lane_addr = tmem + ((uint32_t)(q * 32) << 16) + half * 64;
-        float m1 = -INFINITY, m2 = -INFINITY;
+        float mA = -INFINITY, mB = -INFINITY;
         bool ok = true;
         for (int t = 0; t < ntiles && ok; ++t) {
             const int b = t & 1;
@@ -297,24 +288,25 @@ __global__ void __launch_bounds__(kThreadsTC, 2) k_search_tc(const uint32_t* __r
                     float v[32];
                     tmem_ld32(lane_addr + b * kAccCols + ch * 32, v);
                     if (cols - j0 >= 32)
-                        reduce_chunk<NODUP, false>(v, j0, 32, m1, m2);
+                        reduce_chunk<NODUP, false>(v, j0, 32, mA, mB);
                     else
-                        reduce_chunk<NODUP, true>(v, j0, cols - j0, m1, m2);
+                        reduce_chunk<NODUP, true>(v, j0, cols - j0, mA, mB);
                 }
             }
             fence_before();
             mbar_arrive(smem_u32(&sh.acc_empty[b]));
         }
         if (half == 1)
-            sh.red[q * 32 + lane] = make_float2(m1, m2);
+            sh.red[q * 32 + lane] = make_float2(mA, mB);
         asm volatile("bar.sync 1, %0;" ::"r"(32 * kEpiWarps) : "memory");
         const int c = m0 + q * 32 + lane;
         if (half == 0 && !*abort && c < cols) {
             const float2 r = sh.red[q * 32 + lane];
-            top2_merge<NODUP>(r.x, r.y, m1, m2);
-            const float v1 = ceilf(m1);
-            const int best = (int)((v1 - m1) * 4096.0f);
-            const bool valid = !NODUP || ceilf(m2) != v1;
+            mA = fmaxf(mA, r.x);
+            mB = fmaxf(mB, r.y);
+            const float dA = ceilf(mA);
+            const int best = (int)((dA - mA) * 4096.0f);
+            const bool valid = !NODUP || (int)((mB - floorf(mB)) * 4096.0f) == best;
             if (disp) {
                 int16_t* o = reinterpret_cast<int16_t*>(reinterpret_cast<char*>(disp) + row * disp_pitch);
                 o[c] = valid ? (int16_t)(c - best) : kInvalidDisp;
