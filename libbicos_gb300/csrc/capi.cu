@@ -56,6 +56,15 @@ constexpr int kMaxDevices = 64;
 Scratch g_scratch[kMaxDevices];
 Scratch g_staging[kMaxDevices];  // device copies of host inputs/outputs (bicos_match_host_v1)
 
+// the host path's second stream (row bands alternate between it and the
+// caller's stream) and its fork/join events, per device
+struct HostPipe {
+    std::mutex mu;
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+};
+HostPipe g_host_pipe[kMaxDevices];
+
 // Returns a buffer of >= bytes usable on `st`, ordered after its last use.
 cudaError_t scratch_acquire(Scratch& s, size_t bytes, cudaStream_t st, void** out) {
     if (!s.ev) {
@@ -522,6 +531,13 @@ bicos_status bicos_match_v1(const bicos_image* stack0, const bicos_image* stack1
     return BICOS_OK;
 }
 
+// Host buffers in, host buffers out.  The image is processed in row bands
+// (every stage is row-local, so a band is a bicos_match_v1 call on a
+// sub-image and gives the same rows bit for bit): band k's upload runs on one
+// of two streams while band k-1 computes on the other, each side's band
+// uploaded by one 2-D copy whose rows are whole frame bands (wide rows keep
+// the copy engine near its 1-D rate when the frames of a side are evenly
+// spaced in host memory).  Synchronous on return.
 bicos_status bicos_match_host_v1(const void* const* frames0, const void* const* frames1, uint32_t n, int32_t rows,
                                  int32_t cols, int32_t type, size_t host_step, void* disparity,
                                  size_t disparity_step, void* corrmap, size_t corrmap_step, const bicos_config* cfg,
@@ -549,42 +565,97 @@ bicos_status bicos_match_host_v1(const void* const* frames0, const void* const* 
     if (g.err != cudaSuccess)
         return cuda_fail(g.err, "cudaGetDevice");
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    const size_t plane = align_up((size_t)rows * cols * eb, 256);
-    const size_t disp_bytes = align_up((size_t)rows * cols * elem_bytes_of(dt), 256);
-    const size_t corr_bytes = want_corr ? align_up((size_t)rows * cols * elem_bytes_of(ct), 256) : 0;
+    HostPipe& hp = g_host_pipe[g.dev % kMaxDevices];
+    std::lock_guard<std::mutex> hlk(hp.mu);
+    if (!hp.side) {
+        BICOS_CUDA_TRY(cudaStreamCreateWithFlags(&hp.side, cudaStreamNonBlocking));
+        BICOS_CUDA_TRY(cudaEventCreateWithFlags(&hp.fork, cudaEventDisableTiming));
+        BICOS_CUDA_TRY(cudaEventCreateWithFlags(&hp.join, cudaEventDisableTiming));
+    }
+    const size_t row_bytes = (size_t)cols * eb;
+    const size_t plane = (size_t)rows * row_bytes;  // device frames packed: band copies stay 2-D
+    const size_t disp_row = (size_t)cols * elem_bytes_of(dt);
+    const size_t corr_row = want_corr ? (size_t)cols * elem_bytes_of(ct) : 0;
+    const size_t disp_bytes = align_up((size_t)rows * disp_row, 256);
+    const size_t corr_bytes = align_up((size_t)rows * corr_row, 256);
     Scratch& s = g_staging[g.dev % kMaxDevices];
     std::lock_guard<std::mutex> lk(s.mu);
     void* base = nullptr;
-    BICOS_CUDA_TRY(scratch_acquire(s, 2 * n * plane + disp_bytes + corr_bytes, st, &base));
+    BICOS_CUDA_TRY(scratch_acquire(s, align_up(2 * n * plane, 256) + disp_bytes + corr_bytes, st, &base));
     char* b = static_cast<char*>(base);
-    bicos_image im0[kMaxFrames], im1[kMaxFrames];
-    for (uint32_t t = 0; t < n; ++t) {
-        char* p0 = b + (size_t)t * plane;
-        char* p1 = b + (size_t)(n + t) * plane;
-        BICOS_CUDA_TRY(cudaMemcpy2DAsync(p0, (size_t)cols * eb, frames0[t], host_step, (size_t)cols * eb, rows,
-                                         cudaMemcpyHostToDevice, st));
-        BICOS_CUDA_TRY(cudaMemcpy2DAsync(p1, (size_t)cols * eb, frames1[t], host_step, (size_t)cols * eb, rows,
-                                         cudaMemcpyHostToDevice, st));
-        im0[t] = bicos_image {p0, (size_t)cols * eb, rows, cols, type, 0};
-        im1[t] = bicos_image {p1, (size_t)cols * eb, rows, cols, type, 0};
-    }
-    char* dd = b + 2 * (size_t)n * plane;
+    char* dd = b + align_up(2 * n * plane, 256);
     char* cd = dd + disp_bytes;
-    bicos_image dimg {dd, (size_t)cols * elem_bytes_of(dt), rows, cols, dt, 0};
-    bicos_image cimg {cd, want_corr ? (size_t)cols * elem_bytes_of(ct) : 0, rows, cols, ct, 0};
-    bicos_status rs = bicos_match_v1(im0, im1, n, &dimg, want_corr ? &cimg : nullptr, cfg, stream);
-    if (rs == BICOS_OK) {
-        cudaError_t e = cudaMemcpy2DAsync(disparity, disparity_step, dd, dimg.step, dimg.step, rows,
-                                          cudaMemcpyDeviceToHost, st);
-        if (e == cudaSuccess && want_corr)
-            e = cudaMemcpy2DAsync(corrmap, corrmap_step, cd, cimg.step, cimg.step, rows, cudaMemcpyDeviceToHost, st);
+
+    // a side's frames evenly spaced in host memory: one 2-D copy per band
+    auto spacing = [&](const void* const* f) -> long long {
+        const long long d = (long long)((const char*)f[1] - (const char*)f[0]);
+        for (uint32_t t = 2; t < n; ++t)
+            if ((long long)((const char*)f[t] - (const char*)f[t - 1]) != d)
+                return 0;
+        return d;
+    };
+    const long long sp0 = spacing(frames0), sp1 = spacing(frames1);
+    const bool dense = host_step == row_bytes;
+    const int bands = (size_t)rows * cols * n >= ((size_t)32 << 20) && rows >= 64 ? 4 : 1;
+    const int band_rows = (rows + bands - 1) / bands;
+
+    cudaError_t e = cudaEventRecord(hp.fork, st);
+    if (e == cudaSuccess)
+        e = cudaStreamWaitEvent(hp.side, hp.fork, 0);
+    bicos_status rs = BICOS_OK;
+    for (int k = 0; k < bands && e == cudaSuccess && rs == BICOS_OK; ++k) {
+        const int r0 = k * band_rows, nr = std::min(band_rows, rows - r0);
+        if (nr <= 0)
+            break;
+        cudaStream_t bs = (k & 1) ? hp.side : st;
+        for (int side = 0; side < 2 && e == cudaSuccess; ++side) {
+            const void* const* f = side ? frames1 : frames0;
+            const long long sp = side ? sp1 : sp0;
+            char* dst = b + (size_t)side * n * plane + (size_t)r0 * row_bytes;
+            if (dense && sp >= (long long)plane) {  // the band of every frame: n rows of nr * row_bytes
+                e = cudaMemcpy2DAsync(dst, plane, (const char*)f[0] + (size_t)r0 * host_step, (size_t)sp,
+                                      (size_t)nr * row_bytes, n, cudaMemcpyHostToDevice, bs);
+            } else {
+                for (uint32_t t = 0; t < n && e == cudaSuccess; ++t)
+                    e = dense ? cudaMemcpyAsync(dst + (size_t)t * plane, (const char*)f[t] + (size_t)r0 * host_step,
+                                                (size_t)nr * row_bytes, cudaMemcpyHostToDevice, bs)
+                              : cudaMemcpy2DAsync(dst + (size_t)t * plane, row_bytes,
+                                                  (const char*)f[t] + (size_t)r0 * host_step, host_step, row_bytes, nr,
+                                                  cudaMemcpyHostToDevice, bs);
+            }
+        }
         if (e != cudaSuccess)
-            rs = cuda_fail(e, "cudaMemcpy2DAsync (download)");
+            break;
+        bicos_image im0[kMaxFrames], im1[kMaxFrames];
+        for (uint32_t t = 0; t < n; ++t) {
+            im0[t] = bicos_image {b + (size_t)t * plane + (size_t)r0 * row_bytes, row_bytes, nr, cols, type, 0};
+            im1[t] = bicos_image {b + (size_t)(n + t) * plane + (size_t)r0 * row_bytes, row_bytes, nr, cols, type, 0};
+        }
+        bicos_image dimg {dd + (size_t)r0 * disp_row, disp_row, nr, cols, dt, 0};
+        bicos_image cimg {cd + (size_t)r0 * corr_row, corr_row, nr, cols, ct, 0};
+        rs = bicos_match_v1(im0, im1, n, &dimg, want_corr ? &cimg : nullptr, cfg, bs);
+        if (rs != BICOS_OK)
+            break;
+        auto download = [&](void* host, size_t step, const void* src, size_t row) {
+            char* h = (char*)host + (size_t)r0 * step;
+            return step == row ? cudaMemcpyAsync(h, src, (size_t)nr * row, cudaMemcpyDeviceToHost, bs)
+                               : cudaMemcpy2DAsync(h, step, src, row, row, nr, cudaMemcpyDeviceToHost, bs);
+        };
+        e = download(disparity, disparity_step, dimg.data, disp_row);
+        if (e == cudaSuccess && want_corr)
+            e = download(corrmap, corrmap_step, cimg.data, corr_row);
     }
+    cudaError_t ej = cudaEventRecord(hp.join, hp.side);
+    if (ej == cudaSuccess)
+        ej = cudaStreamWaitEvent(st, hp.join, 0);
     cudaError_t er = scratch_release(s, st);
     cudaError_t es = cudaStreamSynchronize(st);
     if (rs != BICOS_OK)
         return rs;
+    if (e != cudaSuccess)
+        return cuda_fail(e, "bicos_match_host_v1 copies");
+    if (ej != cudaSuccess)
+        return cuda_fail(ej, "bicos_match_host_v1 join");
     if (er != cudaSuccess)
         return cuda_fail(er, "cudaEventRecord");
     if (es != cudaSuccess)

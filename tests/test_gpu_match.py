@@ -179,3 +179,34 @@ def test_streams_and_reuse(cuda, oracle):
     wb, _ = oracle.match(sc_b.left, sc_b.right, _ocfg(oracle, 0.9, 0.1))
     for i, (d, _) in enumerate(outs):
         assert_same(host(d), wa if i % 2 == 0 else wb, f"call {i}")
+
+
+@pytest.mark.parametrize("layout", ["stack", "frames", "pitched"])
+def test_host_path_row_bands_equal_device(cuda, layout):
+    """bicos_match_host_v1 splits images of >= 32 M samples into row bands
+    with overlapped uploads: every layout of the host frames (one evenly
+    spaced stack, separate frame buffers, pitched rows) gives the device
+    path's results bit for bit"""
+    import libbicos_gb300 as lbg
+    from gpu_util import dev, host
+    from libbicos_gb300 import pybicos, scenes
+    sc = scenes.make_scene(1024, 1024, 33, seed=17)
+    c = pybicos.Config()
+    c.nxcorr_threshold = 0.9
+    c.subpixel_step = 0.1
+    c.min_variance = 2.0
+    if layout == "stack":
+        f0, f1 = list(sc.left), list(sc.right)
+    elif layout == "frames":
+        f0 = [np.ascontiguousarray(a) for a in sc.left]
+        f1 = [np.ascontiguousarray(a) for a in sc.right]
+    else:
+        pad0 = np.zeros((33, 1024, 1024 + 40), np.uint8)
+        pad1 = np.zeros((33, 1024, 1024 + 40), np.uint8)
+        pad0[:, :, :1024] = sc.left
+        pad1[:, :, :1024] = sc.right
+        f0, f1 = list(pad0[:, :, :1024]), list(pad1[:, :, :1024])
+    d, corr = pybicos.match(f0, f1, c)
+    wd, wc = lbg.match_device(dev(sc.left, cuda), dev(sc.right, cuda), c)
+    assert_same(d, host(wd), "disparity")
+    assert_same(corr, host(wc), "corrmap")
