@@ -308,6 +308,50 @@ __global__ void __launch_bounds__(kListThreads) k_subpixel_list(const __grid_con
 //    conversion instruction;
 constexpr int kSubThreads = 64;
 
+// Packed FP32 pairs (sm_100+ f32x2 arithmetic): two sweep positions per
+// instruction, each lane rounded like the scalar operation.  Used only where
+// no multiply feeds an add (rounding, sums) or where the reference itself
+// fuses (the FMAs of the second pass): a packed multiply-add chain is not
+// guaranteed to keep the reference's separate roundings, so the interpolant
+// stays scalar.
+typedef unsigned long long f2;
+__device__ __forceinline__ f2 pk(float lo, float hi) {
+    f2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void upk(f2 v, float& lo, float& hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ f2 add2(f2 a, f2 b) {
+    f2 r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2 sub2(f2 a, f2 b) {
+    f2 r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
+    f2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+// round_wrap_f on both lanes
+template<typename T>
+__device__ __forceinline__ f2 round_wrap2(f2 q) {
+    constexpr uint32_t kMask = sizeof(T) == 1 ? 0xFFu : 0xFFFFu;
+    const f2 f = add2(q, pk(12582912.0f, 12582912.0f));
+    uint32_t lo, hi;
+    asm("mov.b64 {%0, %1}, %2;" : "=r"(lo), "=r"(hi) : "l"(f));
+    lo = (lo & kMask) | 0x4B000000u;
+    hi = (hi & kMask) | 0x4B000000u;
+    f2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "r"(lo), "r"(hi));
+    return sub2(r, pk(8388608.0f, 8388608.0f));
+}
+
 __device__ __forceinline__ float nxc_from(float cov, float var0, float var1, bool mv, float minvar) {
     return (mv && (var0 < minvar || var1 < minvar)) ? -1.f : __fdiv_rn(cov, __fsqrt_rn(__fmul_rn(var0, var1)));
 }
@@ -374,46 +418,57 @@ __device__ __forceinline__ void subpixel_f32_body(const AgreeParams& p, int bx, 
                     on[g] = xs <= 1.f;
                     xs = __fadd_rn(xs, p.step);
                 }
-                float iv[XG][NMAX];
-                float s1[XG];
+                constexpr int XP = XG / 2;  // position pairs
+                f2 iv[XP][NMAX];
+                f2 s1[XP];
 #pragma unroll
-                for (int g = 0; g < XG; ++g)
-                    s1[g] = 0.f;
+                for (int q = 0; q < XP; ++q)
+                    s1[q] = 0ull;
 #pragma unroll
                 for (int t = 0; t < NMAX; ++t) {
                     if (t < n) {
                         const float4 k = coef[t * kSubThreads + tid];
 #pragma unroll
-                        for (int g = 0; g < XG; ++g) {
-                            const float q = __fadd_rn(
-                                __fadd_rn(__fmul_rn(__fmul_rn(k.x, xv[g]), xv[g]), __fmul_rn(k.y, xv[g])), k.z);
-                            iv[g][t] = round_wrap_f<T>(q);
-                            s1[g] = __fadd_rn(s1[g], iv[g][t]);
+                        for (int q = 0; q < XP; ++q) {
+                            float v[2];
+#pragma unroll
+                            for (int h = 0; h < 2; ++h) {
+                                const float x = xv[2 * q + h];
+                                v[h] = __fadd_rn(__fadd_rn(__fmul_rn(__fmul_rn(k.x, x), x), __fmul_rn(k.y, x)), k.z);
+                            }
+                            iv[q][t] = round_wrap2<T>(pk(v[0], v[1]));
+                            s1[q] = add2(s1[q], iv[q][t]);
                         }
                     }
                 }
-                float m1[XG], cov[XG], var1[XG];
+                f2 m1[XP], cov[XP], var1[XP];
 #pragma unroll
-                for (int g = 0; g < XG; ++g) {
-                    m1[g] = __fdiv_rn(s1[g], fn);
-                    cov[g] = 0.f;
-                    var1[g] = 0.f;
+                for (int q = 0; q < XP; ++q) {
+                    float lo, hi;
+                    upk(s1[q], lo, hi);
+                    m1[q] = pk(__fdiv_rn(lo, fn), __fdiv_rn(hi, fn));
+                    cov[q] = 0ull;
+                    var1[q] = 0ull;
                 }
 #pragma unroll
                 for (int t = 0; t < NMAX; ++t) {
                     if (t < n) {
                         const float d0 = coef[t * kSubThreads + tid].w;
+                        const f2 D0 = pk(d0, d0);
 #pragma unroll
-                        for (int g = 0; g < XG; ++g) {
-                            const float d1 = __fsub_rn(iv[g][t], m1[g]);
-                            cov[g] = __fmaf_rn(d0, d1, cov[g]);
-                            var1[g] = __fmaf_rn(d1, d1, var1[g]);
+                        for (int q = 0; q < XP; ++q) {
+                            const f2 d1 = sub2(iv[q][t], m1[q]);
+                            cov[q] = fma2(D0, d1, cov[q]);
+                            var1[q] = fma2(d1, d1, var1[q]);
                         }
                     }
                 }
 #pragma unroll
                 for (int g = 0; g < XG; ++g) {
-                    const float nxc = nxc_from(cov[g], var0, var1[g], mv, p.minvar);
+                    float cv_lo, cv_hi, v1_lo, v1_hi;
+                    upk(cov[g / 2], cv_lo, cv_hi);
+                    upk(var1[g / 2], v1_lo, v1_hi);
+                    const float nxc = nxc_from((g & 1) ? cv_hi : cv_lo, var0, (g & 1) ? v1_hi : v1_lo, mv, p.minvar);
                     if (on[g] && best < nxc) {  // NaN never wins
                         best_x = xv[g];
                         best = nxc;
