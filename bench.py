@@ -61,6 +61,24 @@ def dist_env():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0")), ws
 
 
+def max_over_ranks(v, ws, device="cpu"):
+    """The slowest rank's time (a replica run is as fast as its slowest
+    rank); works over NCCL (device = the rank's GPU) and gloo (CPU)."""
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_rate(px_per_rank, seconds, ws):
+    """Whole-job rate of ws replicas each processing px_per_rank in
+    `seconds` (the max over ranks), in Mpx/s."""
+    return ws * px_per_rank / seconds / 1e6
+
+
 def workload_config(double=False):
     return {"workload": f"{WORKLOAD}: 1936x1216 uint8 stereo stack, n=33, limited descriptors (128-bit), "
                         f"threshold {THRESHOLD}, min_variance {MIN_VAR}, subpixel step {STEP}, NoDuplicates, "
@@ -329,12 +347,8 @@ def run_ours(args):
         if ws > 1:
             dist.barrier()
 
-    def max_over_ranks(v):
-        if ws == 1:
-            return v
-        t = torch.tensor([v], dtype=torch.float64, device=device)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    def ranks_max(v):
+        return max_over_ranks(v, ws, device)
 
     def timed(double, steps, warmup, stage_times=False, form=0):
         cfg = cfg_of(double)
@@ -362,7 +376,7 @@ def run_ours(args):
             N.check(L.bicos_stage_times(arr, C.byref(calls)))
             N.check(L.bicos_stage_timing(0))
             st = [arr[i] / max(calls.value, 1) for i in range(3)]
-        return max_over_ranks(ms), st, out
+        return ranks_max(ms), st, out
 
     dev_index = torch.cuda.current_device()
     try:
@@ -373,7 +387,7 @@ def run_ours(args):
     with ClockSampler(smi_dev) as clocks:
         ms, stages, out = timed(False, args.steps, args.warmup, stage_times=True)
     clk = clocks.summary()
-    value = ws * px / (ms * 1e-3) / 1e6
+    value = replica_rate(px, ms * 1e-3, ws)
 
     valid = float(torch.isfinite(out[0]).float().mean().item())
     result = {
@@ -451,7 +465,7 @@ def run_ours(args):
         t0 = time.perf_counter()
         for _ in range(k_e):
             host_call()
-        t_e = max_over_ranks((time.perf_counter() - t0) / k_e)
+        t_e = ranks_max((time.perf_counter() - t0) / k_e)
         result["e2e"] = {"value": round(ws * px / t_e / 1e6, 3), "unit": "Mpx/s",
                          "h2d_bytes_per_step": int(2 * n * px), "d2h_bytes_per_step": int(px * 8),
                          "ms_per_step": round(t_e * 1e3, 3), "api": "bicos_match_host_v1 (pinned host buffers)"}

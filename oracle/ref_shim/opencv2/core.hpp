@@ -16,6 +16,7 @@
 #include <memory>
 #include <stdexcept>
 #include <sys/types.h>
+#include <atomic>
 #include <thread>
 #include <vector>
 
@@ -188,7 +189,10 @@ inline void merge(const std::vector<Mat>& planes, Mat& out) {
     out = m;
 }
 
-// row-range parallel loop over all hardware threads
+// Parallel loop over all hardware threads that hands the body one index at
+// a time, as OpenCV's stripes do for row loops: the reference's bodies
+// allocate per-pixel scratch on the stack (alloca), released only when the
+// body returns, so a body call must not span many image rows.
 inline void parallel_for_(const Range& range, const std::function<void(const Range&)>& body) {
     const int total = range.end - range.start;
     if (total <= 0)
@@ -198,12 +202,13 @@ inline void parallel_for_(const Range& range, const std::function<void(const Ran
         nt = 1;
     if (nt > total)
         nt = total;
+    std::atomic<int> next(range.start);
     std::vector<std::thread> pool;
-    for (int i = 0; i < nt; ++i) {
-        const int b = range.start + (int)((long)total * i / nt);
-        const int e = range.start + (int)((long)total * (i + 1) / nt);
-        pool.emplace_back([b, e, &body]() { body(Range(b, e)); });
-    }
+    for (int i = 0; i < nt; ++i)
+        pool.emplace_back([&]() {
+            for (int r = next++; r < range.end; r = next++)
+                body(Range(r, r + 1));
+        });
     for (auto& t: pool)
         t.join();
 }
