@@ -342,8 +342,8 @@ struct InferSmem {
     // layout with kBChunk.
     alignas(128) uint8_t a[kRowsPT * kH * 2];
     alignas(128) uint8_t b[kH * kH * 2];
-    float4 w1[kH][2];  // unit j: its 7 input weights, then its bias
-    float2 bw[kH];     // unit j of layer 2: bias, output weight
+    float4 w1[kH / 2][4];  // units 2p, 2p+1: (w[2p][i], w[2p+1][i], w[2p][i+1], w[2p+1][i+1]) ..., biases
+    float4 bw[kH / 2];     // units 2p, 2p+1 of layer 2: biases, then output weights
     float norm[2 * kIn];
     float b3;
     alignas(8) uint64_t mbar;
@@ -353,21 +353,64 @@ struct InferSmem {
 
 __device__ __forceinline__ float bf16r(float v) { return __bfloat162float(__float2bfloat16_rn(v)); }
 
+// two floats to BF16 (round to nearest even), lo in the low half
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
-    const uint32_t l = __bfloat16_as_ushort(__float2bfloat16_rn(lo));
-    const uint32_t h = __bfloat16_as_ushort(__float2bfloat16_rn(hi));
-    return l | (h << 16);
+    const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<const uint32_t*>(&v);
+}
+
+// packed FP32 pairs (f32x2): two hidden units per instruction
+typedef unsigned long long f2;
+__device__ __forceinline__ f2 pk(float lo, float hi) {
+    f2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void upk(f2 v, float& lo, float& hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ f2 add2(f2 a, f2 b) {
+    f2 r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2 mul2(f2 a, f2 b) {
+    f2 r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
+    f2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+// gelu_fast on both lanes
+__device__ __forceinline__ f2 gelu2(f2 z) {
+    const f2 hz = mul2(z, pk(0.5f, 0.5f));
+    const f2 u = mul2(z, fma2(mul2(z, z), pk(kGeluC * kGeluA, kGeluC * kGeluA), pk(kGeluC, kGeluC)));
+    float u0, u1;
+    upk(u, u0, u1);
+    return fma2(hz, pk(tanh_fast(u0), tanh_fast(u1)), hz);
 }
 
 // parameters (rounded to BF16) into shared memory, mbarrier, TMEM
 __device__ void infer_setup(InferSmem& S, const float* __restrict__ model) {
     using namespace tc;
     const int tid = threadIdx.x;
-    for (int j = tid; j < kH; j += kRowsPT) {
-        const float* w = model + kW1 + j * kIn;
-        S.w1[j][0] = make_float4(bf16r(w[0]), bf16r(w[1]), bf16r(w[2]), bf16r(w[3]));
-        S.w1[j][1] = make_float4(bf16r(w[4]), bf16r(w[5]), bf16r(w[6]), bf16r(model[kB1 + j]));
-        S.bw[j] = make_float2(bf16r(model[kB2 + j]), bf16r(model[kW3 + j]));
+    for (int p = tid; p < kH / 2; p += kRowsPT) {
+        const float* w0 = model + kW1 + (2 * p) * kIn;
+        const float* w1 = model + kW1 + (2 * p + 1) * kIn;
+        float v[16];
+        for (int i = 0; i < kIn; ++i) {
+            v[2 * i] = bf16r(w0[i]);
+            v[2 * i + 1] = bf16r(w1[i]);
+        }
+        v[14] = bf16r(model[kB1 + 2 * p]);
+        v[15] = bf16r(model[kB1 + 2 * p + 1]);
+        for (int q = 0; q < 4; ++q)
+            S.w1[p][q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+        S.bw[p] = make_float4(bf16r(model[kB2 + 2 * p]), bf16r(model[kB2 + 2 * p + 1]), bf16r(model[kW3 + 2 * p]),
+                              bf16r(model[kW3 + 2 * p + 1]));
     }
     if (tid < 2 * kIn)
         S.norm[tid] = model[kNorm + tid];
@@ -412,25 +455,31 @@ __device__ void infer_teardown(InferSmem& S) {
 __device__ bool infer_tile(InferSmem& S, const float (&x)[kIn], uint32_t phase, float* y) {
     using namespace tc;
     const int tid = threadIdx.x, warp = tid >> 5;
+    f2 X[kIn];
+#pragma unroll
+    for (int i = 0; i < kIn; ++i)
+        X[i] = pk(x[i], x[i]);
+    // layer 1: two units per packed FMA chain
 #pragma unroll 1
     for (int c = 0; c < kH / 8; ++c) {
-        float h[8];
+        uint32_t h[4];
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            const int j = c * 8 + q;
-            const float4 wa = S.w1[j][0], wb = S.w1[j][1];
-            float z = wb.w;
-            z = fmaf(wa.x, x[0], z);
-            z = fmaf(wa.y, x[1], z);
-            z = fmaf(wa.z, x[2], z);
-            z = fmaf(wa.w, x[3], z);
-            z = fmaf(wb.x, x[4], z);
-            z = fmaf(wb.y, x[5], z);
-            z = fmaf(wb.z, x[6], z);
-            h[q] = gelu_fast(z);
+        for (int q = 0; q < 4; ++q) {
+            const int p = c * 4 + q;
+            const float4 w01 = S.w1[p][0], w23 = S.w1[p][1], w45 = S.w1[p][2], w6b = S.w1[p][3];
+            f2 z = pk(w6b.z, w6b.w);
+            z = fma2(pk(w01.x, w01.y), X[0], z);
+            z = fma2(pk(w01.z, w01.w), X[1], z);
+            z = fma2(pk(w23.x, w23.y), X[2], z);
+            z = fma2(pk(w23.z, w23.w), X[3], z);
+            z = fma2(pk(w45.x, w45.y), X[4], z);
+            z = fma2(pk(w45.z, w45.w), X[5], z);
+            z = fma2(pk(w6b.x, w6b.y), X[6], z);
+            float g0, g1;
+            upk(gelu2(z), g0, g1);
+            h[q] = pack_bf16(g0, g1);
         }
-        *reinterpret_cast<uint4*>(S.a + c * kAChunk + tid * 16) =
-            make_uint4(pack_bf16(h[0], h[1]), pack_bf16(h[2], h[3]), pack_bf16(h[4], h[5]), pack_bf16(h[6], h[7]));
+        *reinterpret_cast<uint4*>(S.a + c * kAChunk + tid * 16) = make_uint4(h[0], h[1], h[2], h[3]);
     }
     fence_async_smem();
     fence_before();
@@ -450,19 +499,23 @@ __device__ bool infer_tile(InferSmem& S, const float (&x)[kIn], uint32_t phase, 
     if (__syncthreads_or(!ok))
         return false;
     fence_after();
-    float acc = S.b3;
+    // layer 2 epilogue, two units per packed step; even and odd units
+    // accumulate in the two lanes
+    f2 acc = 0ull;
 #pragma unroll
     for (int half = 0; half < 2; ++half) {
         float v[32];
         tmem_ld32(S.tmem + ((uint32_t)(warp * 32) << 16) + half * 32, v);
 #pragma unroll
-        for (int k = 0; k < 32; ++k) {
-            const float2 bw = S.bw[half * 32 + k];
-            const float z = v[k] + bw.x;
-            acc = fmaf(bw.y, gelu_fast(z), acc);
+        for (int k = 0; k < 32; k += 2) {
+            const float4 bw = S.bw[(half * 32 + k) / 2];
+            const f2 z = add2(pk(v[k], v[k + 1]), pk(bw.x, bw.y));
+            acc = fma2(pk(bw.z, bw.w), gelu2(z), acc);
         }
     }
-    *y = tanhf(acc);
+    float a0, a1;
+    upk(acc, a0, a1);
+    *y = tanhf(S.b3 + (a0 + a1));
     return true;
 }
 
