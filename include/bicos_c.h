@@ -179,6 +179,19 @@ bicos_status bicos_search_v1(const uint32_t* desc0, const uint32_t* desc1, int32
                              int32_t cols, uint32_t nwords, int32_t flags, int32_t max_lr_diff,
                              bicos_image* disparity, bicos_stream_t stream);
 
+/* bicos_search_v1 for descriptors that use only bit positions
+ * 0..bits-1 (1 <= bits <= 32*nwords; LSB-first, bit i in word i/32): the
+ * positions from `bits` on must be zero, as bicos_descriptor_transform_v1
+ * leaves them.  No counterpart in the reference, whose descriptor type
+ * fixes the width.  With bits <= 32*nwords - 2 (every descriptor the
+ * transform writes) the tensor-core search carries each candidate's column
+ * in the two unused top positions, so the product itself is the
+ * first-minimum key.  Outputs equal bicos_search_v1's. */
+bicos_status bicos_search_bits_v1(const uint32_t* desc0, const uint32_t* desc1, int32_t rows,
+                                  int32_t cols, uint32_t nwords, int32_t bits, int32_t flags,
+                                  int32_t max_lr_diff, bicos_image* disparity,
+                                  bicos_stream_t stream);
+
 /*
  * bicos_search_v1 without any device allocation.  No counterpart in the
  * reference: for callers that cannot call cudaMalloc while they run (a

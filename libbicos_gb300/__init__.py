@@ -109,14 +109,21 @@ def descriptor_transform(stack, full: bool, stream=None):
     return out
 
 
-def search(desc0, desc1, flags: int, max_lr_diff: int = -1, stream=None):
-    """Hamming arg-min of (rows, cols, nwords) descriptor tensors -> int16 disparity."""
+def search(desc0, desc1, flags: int, max_lr_diff: int = -1, stream=None, bits=None):
+    """Hamming arg-min of (rows, cols, nwords) descriptor tensors -> int16
+    disparity.  bits: the descriptors' bit count when known (higher bits
+    zero, as the transform writes them; bicos_search_bits_v1)."""
     import torch
     rows, cols, nw = desc0.shape
     out = torch.empty((rows, cols), dtype=torch.int16, device=desc0.device)
     oi = N.tensor_image(out)
-    _raise(N.load().bicos_search_v1(C.c_void_p(desc0.data_ptr()), C.c_void_p(desc1.data_ptr()), rows, cols, nw,
-                                    flags, max_lr_diff, C.byref(oi), _stream_ptr(stream)))
+    lib = N.load()
+    d0, d1 = C.c_void_p(desc0.data_ptr()), C.c_void_p(desc1.data_ptr())
+    if bits is None:
+        _raise(lib.bicos_search_v1(d0, d1, rows, cols, nw, flags, max_lr_diff, C.byref(oi), _stream_ptr(stream)))
+    else:
+        _raise(lib.bicos_search_bits_v1(d0, d1, rows, cols, nw, int(bits), flags, max_lr_diff, C.byref(oi),
+                                        _stream_ptr(stream)))
     return out
 
 

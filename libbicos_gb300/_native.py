@@ -86,6 +86,7 @@ def load():
         "bicos_stage_times": ([C.POINTER(C.c_float), C.POINTER(I)], C.c_int),
         "bicos_descriptor_transform_v1": ([IMG, U, I, U, P, P], C.c_int),
         "bicos_search_v1": ([P, P, I, I, U, I, I, IMG, P], C.c_int),
+        "bicos_search_bits_v1": ([P, P, I, I, U, I, I, I, IMG, P], C.c_int),
         "bicos_search_noalloc_v1": ([P, P, I, I, U, I, I, IMG, P], C.c_int),
         "bicos_agree_v1": ([IMG, IMG, IMG, U, F, I, F, I, IMG, P], C.c_int),
         "bicos_agree_subpixel_v1": ([IMG, IMG, IMG, U, F, F, I, F, I, IMG, IMG, P], C.c_int),

@@ -149,6 +149,14 @@ int elem_bytes_of(int type) {
 
 int required_bits(int n, bool full) { return full ? n * n - 2 * n + 3 : 4 * n - 7; }
 
+// bit positions the transform writes (0 .. positions-1): the full layout
+// fills exactly required_bits; the limited layout (3 bits per step, n-4
+// pair-sum bits, 4 tail bits: include/impl/cpu/descriptor_transform.hpp:
+// 32-73) ends one position past the reference's count
+int descriptor_positions(int n, bool full) {
+    return full ? required_bits(n, true) : 3 * (n - 2) + std::max(0, n - 4) + 4;
+}
+
 int words_for(int n, bool full, int max_bits) {
     const int bits = required_bits(n, full);
     if (bits <= 32) return 1;
@@ -343,14 +351,16 @@ cudaError_t bicos_gb300::enqueue_transform(const MatchPlan& P, const MatchBuffer
 }
 
 cudaError_t bicos_gb300::enqueue_search(const MatchPlan& P, const MatchBuffers& m, cudaStream_t st) {
+    const int bits = descriptor_positions(P.n, P.full);
     if (P.consistency) {
-        cudaError_t e = launch_search(m.d0, m.d1, P.rows, P.cols, P.nw, P.cfg->no_dupes != 0, 2, nullptr, 0, m.fwd,
-                                      m.rev, st);
+        cudaError_t e = launch_search(m.d0, m.d1, P.rows, P.cols, P.nw, bits, P.cfg->no_dupes != 0, 2, nullptr, 0,
+                                      m.fwd, m.rev, st);
         if (e == cudaSuccess)
             e = launch_consistency(m.fwd, m.rev, P.rows, P.cols, P.cfg->max_lr_diff, m.raw, m.raw_pitch, st);
         return e;
     }
-    return launch_search(m.d0, m.d1, P.rows, P.cols, P.nw, true, 1, m.raw, m.raw_pitch, nullptr, nullptr, st);
+    return launch_search(m.d0, m.d1, P.rows, P.cols, P.nw, bits, true, 1, m.raw, m.raw_pitch, nullptr, nullptr,
+                         st);
 }
 
 AgreeParams bicos_gb300::agree_params(const MatchPlan& P, const MatchBuffers& m) {
@@ -685,13 +695,17 @@ bicos_status bicos_descriptor_transform_v1(const bicos_image* stack, uint32_t n,
     return BICOS_OK;
 }
 
-bicos_status bicos_search_v1(const uint32_t* desc0, const uint32_t* desc1, int32_t rows, int32_t cols,
-                             uint32_t nwords, int32_t flags, int32_t max_lr_diff, bicos_image* disparity,
-                             bicos_stream_t stream) {
+namespace {
+
+bicos_status search_stage(const uint32_t* desc0, const uint32_t* desc1, int32_t rows, int32_t cols,
+                          uint32_t nwords, int bits, int32_t flags, int32_t max_lr_diff, bicos_image* disparity,
+                          bicos_stream_t stream) {
     if (!desc0 || !desc1 || rows < 1 || cols < 1 || cols > 32767)
         return fail(BICOS_ERR_INVALID_ARGUMENT, "bad descriptor arguments");
     if (nwords != 1 && nwords != 2 && nwords != 4 && nwords != 8 && nwords != 12 && nwords != 16)
         return fail(BICOS_ERR_INVALID_ARGUMENT, "unsupported descriptor width");
+    if (bits < 0 || bits > 32 * (int)nwords)
+        return fail(BICOS_ERR_INVALID_ARGUMENT, "descriptor bit count out of range");
     if (!image_ok(disparity, rows, cols, BICOS_16S))
         return fail(BICOS_ERR_EXCEPTION, "disparity must be an int16 image of the descriptor size");
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
@@ -708,7 +722,7 @@ bicos_status bicos_search_v1(const uint32_t* desc0, const uint32_t* desc1, int32
         BICOS_CUDA_TRY(scratch_acquire(s, 2 * bb, st, &base));
         int32_t* fwd = static_cast<int32_t*>(base);
         int32_t* rev = reinterpret_cast<int32_t*>(static_cast<char*>(base) + bb);
-        e = launch_search(desc0, desc1, rows, cols, (int)nwords, nodup, 2, nullptr, 0, fwd, rev, st);
+        e = launch_search(desc0, desc1, rows, cols, (int)nwords, bits, nodup, 2, nullptr, 0, fwd, rev, st);
         if (e == cudaSuccess)
             e = launch_consistency(fwd, rev, rows, cols, max_lr_diff, static_cast<int16_t*>(disparity->data),
                                    (long long)disparity->step, st);
@@ -716,12 +730,28 @@ bicos_status bicos_search_v1(const uint32_t* desc0, const uint32_t* desc1, int32
         if (e == cudaSuccess)
             e = er;
     } else {
-        e = launch_search(desc0, desc1, rows, cols, (int)nwords, nodup, 1, static_cast<int16_t*>(disparity->data),
+        e = launch_search(desc0, desc1, rows, cols, (int)nwords, bits, nodup, 1, static_cast<int16_t*>(disparity->data),
                           (long long)disparity->step, nullptr, nullptr, st);
     }
     if (e != cudaSuccess)
         return cuda_fail(e, "search launch");
     return BICOS_OK;
+}
+
+}  // namespace
+
+bicos_status bicos_search_v1(const uint32_t* desc0, const uint32_t* desc1, int32_t rows, int32_t cols,
+                             uint32_t nwords, int32_t flags, int32_t max_lr_diff, bicos_image* disparity,
+                             bicos_stream_t stream) {
+    return search_stage(desc0, desc1, rows, cols, nwords, 0, flags, max_lr_diff, disparity, stream);
+}
+
+bicos_status bicos_search_bits_v1(const uint32_t* desc0, const uint32_t* desc1, int32_t rows, int32_t cols,
+                                  uint32_t nwords, int32_t bits, int32_t flags, int32_t max_lr_diff,
+                                  bicos_image* disparity, bicos_stream_t stream) {
+    if (bits < 1)
+        return fail(BICOS_ERR_INVALID_ARGUMENT, "descriptor bit count out of range");
+    return search_stage(desc0, desc1, rows, cols, nwords, bits, flags, max_lr_diff, disparity, stream);
 }
 
 bicos_status bicos_agree_v1(bicos_image* disparity, const bicos_image* stack0, const bicos_image* stack1,

@@ -64,8 +64,10 @@ cudaError_t launch_transform(const StackParams& p, int sides, bool full, int nwo
 // Row-wise arg-min.  When disp != nullptr (one direction, NODUPES or plain)
 // the kernel writes int16 disparities col0 - best directly; otherwise it
 // writes int32 best columns (-1 = invalid) of each direction to best0/best1.
+// bits: the descriptors' bit count when known (the transform's), else 0
+// (every bit of the nwords words may be set).
 cudaError_t launch_search(const uint32_t* desc0, const uint32_t* desc1, int rows, int cols,
-                          int nwords, bool nodupes, int directions, int16_t* disp,
+                          int nwords, int bits, bool nodupes, int directions, int16_t* disp,
                           long long disp_pitch, int32_t* best0, int32_t* best1,
                           cudaStream_t st);
 
@@ -73,7 +75,7 @@ cudaError_t launch_search(const uint32_t* desc0, const uint32_t* desc1, int rows
 // rows of at most 4096 columns
 bool search_tc_supported(int cols);
 cudaError_t launch_search_tc(const uint32_t* desc0, const uint32_t* desc1, int rows, int cols, int nwords,
-                             bool nodupes, int directions, int16_t* disp, long long disp_pitch,
+                             int bits, bool nodupes, int directions, int16_t* disp, long long disp_pitch,
                              int32_t* best0, int32_t* best1, cudaStream_t st);
 // number of tensor-core search CTAs whose bounded waits ran out (synchronous)
 unsigned int read_tc_faults();

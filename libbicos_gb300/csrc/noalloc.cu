@@ -97,13 +97,13 @@ extern "C" bicos_status bicos_search_noalloc_v1(const uint32_t* desc0, const uin
             return noalloc_fail(BICOS_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
         int32_t* fwd = base;
         int32_t* rev = base + kNoAllocMaxPixels;
-        e = launch_search(desc0, desc1, rows, cols, (int)nwords, nodup, 2, nullptr, 0, fwd, rev, st);
+        e = launch_search(desc0, desc1, rows, cols, (int)nwords, 0, nodup, 2, nullptr, 0, fwd, rev, st);
         if (e == cudaSuccess)
             e = launch_consistency(fwd, rev, rows, cols, max_lr_diff, static_cast<int16_t*>(disparity->data),
                                    (long long)disparity->step, st);
     } else {
         // no scratch in this form: the kernel writes the disparity directly
-        e = launch_search(desc0, desc1, rows, cols, (int)nwords, nodup, 1, static_cast<int16_t*>(disparity->data),
+        e = launch_search(desc0, desc1, rows, cols, (int)nwords, 0, nodup, 1, static_cast<int16_t*>(disparity->data),
                           (long long)disparity->step, nullptr, nullptr, st);
     }
     if (e != cudaSuccess)

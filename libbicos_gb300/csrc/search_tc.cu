@@ -12,9 +12,21 @@
 //   keeps the two largest keys  key = dot - col * 2^-12  (exact in FP32 for
 //   cols <= 4096), which carry the first arg-max and the tie test of
 //   libBICOS's bicos_search (include/impl/cpu/bicos.hpp:50-76).
+// Column-coded form (descriptors using at most 32*NW-2 bit positions, the
+// match path's): the two top K slots of every row are padding, so they
+// carry the candidate's column within its pair of tiles (c = 0..255)
+// instead, and the MMA itself yields
+//   D = 128 * dot' - c   (dot' = the sum over the other 32*NW-2 slots,
+//   even; descriptor slots +-16 (queries) x +-8 (candidates), code slots
+//   -1, -16 in the query row against c's two nibbles in the candidate row)
+// -- the first-arg-max key within a tile pair with no per-candidate
+// arithmetic (integers below 2^17, exact in the FP32 accumulator).  The
+// epilogue decodes each pair's maxima into global keys once per pair.
 // Outputs and semantics are those of k_search (search.cu).  All waits are
 // bounded: a wait that runs out records a fault, and the CTA frees its TMEM
 // and exits.
+#include <climits>
+
 #include "kernels.cuh"
 #include "tcgen05.cuh"
 
@@ -36,10 +48,34 @@ constexpr int kMaxCols = 4096;      // key exactness bound
 constexpr uint32_t kChunkBytes = 128 * 16;  // one 16-byte K chunk of 128 rows
 constexpr uint32_t kIdesc = tc::idesc_f8_e4m3(kRows, kRows);
 
-// 8 descriptor bits -> 8 FP8 values (+1 set, -1 clear)
-__device__ __forceinline__ uint32_t expand_nibble(uint32_t x) {
-    const uint32_t s = (x * 0x204081u) & 0x01010101u;  // bit i -> byte i
-    return 0xB8B8B8B8u - (s << 7);
+// FP8 patterns of a clear bit (a set bit flips bit 7, the sign): +-1, and
+// in the column-coded form +-16 (query rows) and +-8 (candidate rows)
+constexpr uint32_t kClearPlain = 0xB8B8B8B8u;
+constexpr uint32_t kClearQuery = 0xD8D8D8D8u;
+constexpr uint32_t kClearCand = 0xD0D0D0D0u;
+
+// bits 0..3 (lo) or 4..7 (hi) of x -> 4 FP8 bytes: the product puts nibble
+// bit i at bit 8i+7 (the four shifted copies of the nibble do not overlap,
+// so nothing carries), the mask keeps those bits, the XOR applies them to
+// the clear pattern's sign bits
+__device__ __forceinline__ uint32_t fp8_lo(uint32_t x, uint32_t clear4) {
+    return (((x & 0xFu) * 0x10204080u) & 0x80808080u) ^ clear4;
+}
+__device__ __forceinline__ uint32_t fp8_hi(uint32_t x, uint32_t clear4) {
+    return (((x & 0xF0u) * 0x01020408u) & 0x80808080u) ^ clear4;
+}
+
+// e4m3 encoding of the integers 0..15 (exact: at most 4 significant bits)
+__device__ __forceinline__ uint32_t e4m3_small(uint32_t v) {
+    const uint32_t e = 31u - __clz(v | 1u);
+    return v ? ((e + 7u) << 3) | ((v << (3u - e)) & 7u) : 0u;
+}
+
+// byte lanes 2..3 of a row's last 4 K slots: the query row's code factors
+// -1, -16 and a candidate's column nibbles (c < 256)
+constexpr uint32_t kQueryCode = 0xD8B80000u;
+__device__ __forceinline__ uint32_t column_code(uint32_t c) {
+    return (e4m3_small(c & 15u) << 16) | (e4m3_small(c >> 4) << 24);
 }
 
 // one descriptor's words, loaded ahead of its expansion
@@ -70,20 +106,24 @@ __device__ __forceinline__ Desc<NW> load_desc(const uint32_t* p) {
     return d;
 }
 
-// one descriptor into row rr of a 128-row FP8 tile (canonical layout);
-// lut: 16 words, nibble -> 4 FP8 values, one word per bank, so the
-// warp's lookups never conflict
-template<int NW>
-__device__ __forceinline__ void expand_desc(uint8_t* tile, int rr, const Desc<NW>& d, const uint32_t* lut) {
+// one descriptor into row rr of a 128-row FP8 tile (canonical layout).
+// code (column-coded form): bytes 2..3 of the row's last 4 K slots,
+// replacing the padding bits there.
+template<int NW, bool ENC>
+__device__ __forceinline__ void expand_desc(uint8_t* tile, int rr, const Desc<NW>& d, uint32_t clear4,
+                                            uint32_t code = 0) {
     uint8_t* base = tile + (rr >> 3) * 128 + (rr & 7) * 16;
 #pragma unroll
     for (int w = 0; w < NW; ++w) {
         const uint32_t x = d.w[w];
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
-            const uint32_t y = x >> (16 * h);
+            const uint32_t y = x >> (16 * h), z = y >> 8;
+            uint32_t top = fp8_hi(z, clear4);
+            if (ENC && w == NW - 1 && h == 1)
+                top = (top & 0xFFFFu) | code;
             *reinterpret_cast<uint4*>(base + (2 * w + h) * kChunkBytes) =
-                make_uint4(lut[y & 0xFu], lut[(y >> 4) & 0xFu], lut[(y >> 8) & 0xFu], lut[(y >> 12) & 0xFu]);
+                make_uint4(fp8_lo(y, clear4), fp8_hi(y, clear4), fp8_lo(z, clear4), top);
         }
     }
 }
@@ -135,6 +175,58 @@ __device__ __forceinline__ void reduce_chunk(const float (&v)[32], int j0, int l
         mB = fmax3(mB, fmax3(cb[0], cb[1], cb[2]) + off, cb[3] + off);
 }
 
+// The same reduction over column-coded keys (D = 128 * dot' - c, c the
+// column within the tile pair): chain A is the plain maximum of D; chain B
+// (with no-duplicates) keeps max(D + 2c) = 128 * dot' + c.  c0: the
+// chunk's first c.  Per pair of candidates: 1 three-input maximum, plus
+// (no-duplicates) 2 FADDs and 1 more maximum.
+template<bool NODUP, bool MASKED>
+__device__ __forceinline__ void reduce_chunk_coded(const float (&v)[32], int c0, int lim, float& kA, float& kB) {
+    float ca[4], cb[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+        ca[i] = cb[i] = -INFINITY;
+#pragma unroll
+    for (int k = 0; k < 32; k += 2) {
+        float a = v[k], b = v[k + 1];
+        float a2 = a + (float)(2 * k);
+        float b2 = b + (float)(2 * k + 2);
+        if constexpr (MASKED) {
+            a = k < lim ? a : -INFINITY;
+            b = k + 1 < lim ? b : -INFINITY;
+            a2 = k < lim ? a2 : -INFINITY;
+            b2 = k + 1 < lim ? b2 : -INFINITY;
+        }
+        const int i = (k >> 1) & 3;
+        ca[i] = fmax3(ca[i], a, b);
+        if constexpr (NODUP)
+            cb[i] = fmax3(cb[i], a2, b2);
+    }
+    kA = fmax3(kA, fmax3(ca[0], ca[1], ca[2]), ca[3]);
+    if constexpr (NODUP) {
+        const float off = (float)(2 * c0);
+        kB = fmax3(kB, fmax3(cb[0], cb[1], cb[2]) + off, cb[3] + off);
+    }
+}
+
+// a tile pair's coded maxima -> global integer keys 8192 * e - j (chain A,
+// first column) and 8192 * e + j (chain B, last column), e = dot' / 2,
+// j = 256 * pair + c; merged into the running maxima
+template<bool NODUP>
+__device__ __forceinline__ void merge_pair(float& kA, float& kB, int pair, int& gA, int& gB) {
+    if (kA > -INFINITY) {
+        const int a = (int)kA;
+        const int c = (-a) & 255;
+        gA = max(gA, ((a + c) >> 8) * 8192 - (pair * 256 + c));
+        if constexpr (NODUP) {
+            const int b = (int)kB;
+            const int cb = b & 255;
+            gB = max(gB, ((b - cb) >> 8) * 8192 + (pair * 256 + cb));
+        }
+    }
+    kA = kB = -INFINITY;
+}
+
 // Warp roles of the pipelined CTA (one CTA = one row x 128 query pixels):
 //   warps 0..7   epilogue: warp w reads TMEM lane quarter w%4, columns
 //                [64*(w/4), 64*(w/4)+64) of each accumulator
@@ -164,7 +256,7 @@ struct TcShared {
     float2 red[kRows];      // second column half's (chain A, chain B) maxima per query
 };
 
-template<int NW, bool NODUP>
+template<int NW, bool NODUP, bool ENC>
 __global__ void __launch_bounds__(kThreadsTC, 2) k_search_tc(const uint32_t* __restrict__ d0,
                                                              const uint32_t* __restrict__ d1, int rows, int cols,
                                                              int16_t* __restrict__ disp, long long disp_pitch,
@@ -177,7 +269,6 @@ __global__ void __launch_bounds__(kThreadsTC, 2) k_search_tc(const uint32_t* __r
     extern __shared__ __align__(1024) uint8_t smem[];
     uint8_t* sA = smem;
     uint8_t* sB = smem + TILE;  // STAGES buffers
-    uint32_t* lut = reinterpret_cast<uint32_t*>(smem + (1 + STAGES) * TILE);
     __shared__ TcShared sh;
     volatile int* abort = &sh.abort;
 
@@ -189,8 +280,6 @@ __global__ void __launch_bounds__(kThreadsTC, 2) k_search_tc(const uint32_t* __r
     const uint32_t* crow = (dir ? d0 : d1) + row_off;
     const int ntiles = (cols + kRows - 1) / kRows;
 
-    if (tid < 16)
-        lut[tid] = expand_nibble(tid);
     if (warp == 0) {
         tmem_alloc(smem_u32(&sh.tmem), 2 * kAccCols);
         tmem_relinquish();
@@ -248,7 +337,8 @@ __global__ void __launch_bounds__(kThreadsTC, 2) k_search_tc(const uint32_t* __r
 #pragma unroll
         for (int i = 0; i < PF; ++i)
             ring[i] = cand(i);
-        expand_desc<NW>(sA, p, load_desc<NW>(qrow + (size_t)min(m0 + p, cols - 1) * NW), lut);
+        expand_desc<NW, ENC>(sA, p, load_desc<NW>(qrow + (size_t)min(m0 + p, cols - 1) * NW),
+                             ENC ? kClearQuery : kClearPlain, kQueryCode);
         bool live = true;
         for (int t0 = 0; t0 < ntiles && live; t0 += PF) {
 #pragma unroll
@@ -263,7 +353,8 @@ __global__ void __launch_bounds__(kThreadsTC, 2) k_search_tc(const uint32_t* __r
                     live = false;
                     break;
                 }
-                expand_desc<NW>(sB + slot * TILE, p, cur, lut);
+                expand_desc<NW, ENC>(sB + slot * TILE, p, cur, ENC ? kClearCand : kClearPlain,
+                                     ENC ? column_code((t & 1) * kRows + p) : 0u);
                 fence_async_smem();
                 mbar_arrive(smem_u32(&sh.full_b[slot]));
             }
@@ -273,6 +364,7 @@ __global__ void __launch_bounds__(kThreadsTC, 2) k_search_tc(const uint32_t* __r
         const int q = warp & 3, half = warp >> 2;
         const uint32_t lane_addr = tmem + ((uint32_t)(q * 32) << 16) + half * 64;
         float mA = -INFINITY, mB = -INFINITY;
+        int gA = INT_MIN, gB = INT_MIN;  // column-coded form: global keys
         bool ok = true;
         for (int t = 0; t < ntiles && ok; ++t) {
             const int b = t & 1;
@@ -287,26 +379,48 @@ __global__ void __launch_bounds__(kThreadsTC, 2) k_search_tc(const uint32_t* __r
                 if (j0 < cols) {
                     float v[32];
                     tmem_ld32(lane_addr + b * kAccCols + ch * 32, v);
-                    if (cols - j0 >= 32)
-                        reduce_chunk<NODUP, false>(v, j0, 32, mA, mB);
-                    else
-                        reduce_chunk<NODUP, true>(v, j0, cols - j0, mA, mB);
+                    if constexpr (ENC) {
+                        const int c0 = (t & 1) * kRows + half * 64 + ch * 32;
+                        if (cols - j0 >= 32)
+                            reduce_chunk_coded<NODUP, false>(v, c0, 32, mA, mB);
+                        else
+                            reduce_chunk_coded<NODUP, true>(v, c0, cols - j0, mA, mB);
+                    } else {
+                        if (cols - j0 >= 32)
+                            reduce_chunk<NODUP, false>(v, j0, 32, mA, mB);
+                        else
+                            reduce_chunk<NODUP, true>(v, j0, cols - j0, mA, mB);
+                    }
                 }
             }
             fence_before();
             mbar_arrive(smem_u32(&sh.acc_empty[b]));
+            if (ENC && ((t & 1) || t == ntiles - 1))
+                merge_pair<NODUP>(mA, mB, t >> 1, gA, gB);
         }
-        if (half == 1)
-            sh.red[q * 32 + lane] = make_float2(mA, mB);
+        if (half == 1) {
+            if constexpr (ENC)
+                sh.red[q * 32 + lane] = make_float2(__int_as_float(gA), __int_as_float(gB));
+            else
+                sh.red[q * 32 + lane] = make_float2(mA, mB);
+        }
         asm volatile("bar.sync 1, %0;" ::"r"(32 * kEpiWarps) : "memory");
         const int c = m0 + q * 32 + lane;
         if (half == 0 && !*abort && c < cols) {
             const float2 r = sh.red[q * 32 + lane];
-            mA = fmaxf(mA, r.x);
-            mB = fmaxf(mB, r.y);
-            const float dA = ceilf(mA);
-            const int best = (int)((dA - mA) * 4096.0f);
-            const bool valid = !NODUP || (int)((mB - floorf(mB)) * 4096.0f) == best;
+            int best;
+            bool valid;
+            if constexpr (ENC) {
+                gA = max(gA, __float_as_int(r.x));
+                gB = max(gB, __float_as_int(r.y));
+                best = (-gA) & 8191;
+                valid = !NODUP || (gB & 8191) == best;
+            } else {
+                mA = fmaxf(mA, r.x);
+                mB = fmaxf(mB, r.y);
+                best = (int)((ceilf(mA) - mA) * 4096.0f);
+                valid = !NODUP || (int)((mB - floorf(mB)) * 4096.0f) == best;
+            }
             if (disp) {
                 int16_t* o = reinterpret_cast<int16_t*>(reinterpret_cast<char*>(disp) + row * disp_pitch);
                 o[c] = valid ? (int16_t)(c - best) : kInvalidDisp;
@@ -327,12 +441,13 @@ __global__ void __launch_bounds__(kThreadsTC, 2) k_search_tc(const uint32_t* __r
 }
 
 template<int NW, bool NODUP>
-cudaError_t launch_tc_nw(const uint32_t* d0, const uint32_t* d1, int rows, int cols, int dirs, int16_t* disp,
-                         long long disp_pitch, int32_t* b0, int32_t* b1, cudaStream_t st) {
+cudaError_t launch_tc_nw(const uint32_t* d0, const uint32_t* d1, int rows, int cols, int bits, int dirs,
+                         int16_t* disp, long long disp_pitch, int32_t* b0, int32_t* b1, cudaStream_t st) {
     constexpr int TILE = kRows * NW * 32;
     // at least 80 KB per CTA: at most 2 CTAs (2 x 256 TMEM columns) per SM
-    const size_t smem = max((size_t)(1 + b_stages<NW>()) * TILE + 64, (size_t)80 * 1024);
-    auto k = k_search_tc<NW, NODUP>;
+    const size_t smem = max((size_t)(1 + b_stages<NW>()) * TILE, (size_t)80 * 1024);
+    // column-coded when the two top K slots are padding
+    auto k = bits >= 1 && bits <= 32 * NW - 2 ? k_search_tc<NW, NODUP, true> : k_search_tc<NW, NODUP, false>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess)
         return e;
@@ -342,15 +457,16 @@ cudaError_t launch_tc_nw(const uint32_t* d0, const uint32_t* d1, int rows, int c
 }
 
 template<bool NODUP>
-cudaError_t launch_tc_dup(const uint32_t* d0, const uint32_t* d1, int rows, int cols, int nwords, int dirs,
-                          int16_t* disp, long long disp_pitch, int32_t* b0, int32_t* b1, cudaStream_t st) {
+cudaError_t launch_tc_dup(const uint32_t* d0, const uint32_t* d1, int rows, int cols, int nwords, int bits,
+                          int dirs, int16_t* disp, long long disp_pitch, int32_t* b0, int32_t* b1,
+                          cudaStream_t st) {
     switch (nwords) {
-        case 1: return launch_tc_nw<1, NODUP>(d0, d1, rows, cols, dirs, disp, disp_pitch, b0, b1, st);
-        case 2: return launch_tc_nw<2, NODUP>(d0, d1, rows, cols, dirs, disp, disp_pitch, b0, b1, st);
-        case 4: return launch_tc_nw<4, NODUP>(d0, d1, rows, cols, dirs, disp, disp_pitch, b0, b1, st);
-        case 8: return launch_tc_nw<8, NODUP>(d0, d1, rows, cols, dirs, disp, disp_pitch, b0, b1, st);
-        case 12: return launch_tc_nw<12, NODUP>(d0, d1, rows, cols, dirs, disp, disp_pitch, b0, b1, st);
-        case 16: return launch_tc_nw<16, NODUP>(d0, d1, rows, cols, dirs, disp, disp_pitch, b0, b1, st);
+        case 1: return launch_tc_nw<1, NODUP>(d0, d1, rows, cols, bits, dirs, disp, disp_pitch, b0, b1, st);
+        case 2: return launch_tc_nw<2, NODUP>(d0, d1, rows, cols, bits, dirs, disp, disp_pitch, b0, b1, st);
+        case 4: return launch_tc_nw<4, NODUP>(d0, d1, rows, cols, bits, dirs, disp, disp_pitch, b0, b1, st);
+        case 8: return launch_tc_nw<8, NODUP>(d0, d1, rows, cols, bits, dirs, disp, disp_pitch, b0, b1, st);
+        case 12: return launch_tc_nw<12, NODUP>(d0, d1, rows, cols, bits, dirs, disp, disp_pitch, b0, b1, st);
+        case 16: return launch_tc_nw<16, NODUP>(d0, d1, rows, cols, bits, dirs, disp, disp_pitch, b0, b1, st);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -360,14 +476,14 @@ cudaError_t launch_tc_dup(const uint32_t* d0, const uint32_t* d1, int rows, int 
 bool search_tc_supported(int cols) { return cols >= 1 && cols <= kMaxCols; }
 
 cudaError_t launch_search_tc(const uint32_t* desc0, const uint32_t* desc1, int rows, int cols, int nwords,
-                             bool nodupes, int directions, int16_t* disp, long long disp_pitch, int32_t* best0,
-                             int32_t* best1, cudaStream_t st) {
+                             int bits, bool nodupes, int directions, int16_t* disp, long long disp_pitch,
+                             int32_t* best0, int32_t* best1, cudaStream_t st) {
     if (!search_tc_supported(cols) || rows < 1)
         return cudaErrorInvalidValue;
-    return nodupes ? launch_tc_dup<true>(desc0, desc1, rows, cols, nwords, directions, disp, disp_pitch, best0,
-                                         best1, st)
-                   : launch_tc_dup<false>(desc0, desc1, rows, cols, nwords, directions, disp, disp_pitch, best0,
-                                          best1, st);
+    return nodupes ? launch_tc_dup<true>(desc0, desc1, rows, cols, nwords, bits, directions, disp, disp_pitch,
+                                         best0, best1, st)
+                   : launch_tc_dup<false>(desc0, desc1, rows, cols, nwords, bits, directions, disp, disp_pitch,
+                                          best0, best1, st);
 }
 
 unsigned int read_tc_faults() {

@@ -83,6 +83,31 @@ def test_edge_stack_sizes(cuda, oracle, n, full):
         assert_same(host(corr), wc, f"n={n} corr")
 
 
+@pytest.mark.parametrize("n", [9, 17, 33])
+def test_periodic_texture_ties(cuda, oracle, n):
+    """column-periodic stacks (every descriptor repeats every 7 columns) on
+    4096-column rows: the search's column-coded keys must pick the
+    reference's first minimum and flag every duplicate (n = 9, 17, 33 use
+    30, 62 and 126 of 32, 64 and 128 bit positions: exactly the two spare
+    slots the code needs)"""
+    rng = np.random.default_rng(n)
+    base = rng.integers(0, 256, size=(n, 1, 7), dtype=np.uint8)
+    left = np.tile(base, (1, 3, 586))[:, :, :4096].copy()
+    right = np.roll(left, 3, axis=2).copy()
+    left[:, 1, 1000] ^= 0x55  # one unique texel in the middle row
+    # binary random frames: many partial ties
+    bl = rng.integers(0, 2, size=(n, 2, 4096), dtype=np.uint8)
+    br = np.roll(bl, 5, axis=2).copy()
+    for sl, sr in ((left, right), (bl, br)):
+        for cons in (None, (1, False), (2, True)):
+            for thr in (None, 0.5):
+                d, corr = lbg.match_device(dev(sl, cuda), dev(sr, cuda), py_cfg(thr, cons=cons))
+                wd, wc = oracle.match(sl, sr, _ocfg(oracle, thr, cons=cons))
+                assert_same(host(d), wd, f"n={n} cons={cons} thr={thr}")
+                if thr is not None:
+                    assert_same(host(corr), wc, f"n={n} cons={cons} corr")
+
+
 def test_no_threshold_returns_raw_int16(cuda, oracle):
     sc = scenes.make_scene(16, 120, 8, seed=5)
     d, corr = lbg.match_device(dev(sc.left, cuda), dev(sc.right, cuda), py_cfg(None))

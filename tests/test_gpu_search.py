@@ -26,6 +26,53 @@ def test_search_vs_oracle(cuda, oracle, nw, flags):
             assert_same(got, oracle.search(d0, d1, flags, lr), f"nw={nw} flags={flags} bits={bits} lr={lr}")
 
 
+@pytest.mark.parametrize("nw", [1, 2, 4, 8, 12, 16])
+@pytest.mark.parametrize("flags", [0, 1, 2, 3])
+def test_search_declared_bits_vs_oracle(cuda, oracle, nw, flags):
+    """bicos_search_bits_v1: with at most 32*nw-2 bit positions the
+    tensor-core search takes its column-coded form (the candidate's column
+    in the top two slots of the FP8 operands); tie-heavy value ranges and
+    rows of up to 4096 columns (every tile pair), the declared count at the
+    bound and below it"""
+    rng = np.random.default_rng(nw * 100 + flags)
+    for bits, cols, rows in ((1, 4096, 2), (2, 1000, 3), (4, 257, 7), (8, 300, 7), (29, 129, 5)):
+        d0, d1 = _desc(rng, rows, cols, nw, bits), _desc(rng, rows, cols, nw, bits)
+        for declared in (32 * nw - 2, 32 * (nw - 1) + bits):
+            for lr in (0, 2):
+                got = host(lbg.search(dev(d0.view(np.int32), cuda), dev(d1.view(np.int32), cuda), flags, lr,
+                                      bits=declared))
+                assert_same(got, oracle.search(d0, d1, flags, lr),
+                            f"nw={nw} flags={flags} bits={bits} declared={declared} lr={lr}")
+
+
+def test_search_declared_bits_all_ties(cuda, oracle):
+    """every candidate ties (identical descriptors): first column without
+    no-duplicates, invalid with it; and one unique best per row at the
+    far end of a 4096-column row"""
+    for nw in (1, 4, 16):
+        d = np.zeros((2, 4096, nw), np.uint32)
+        d[:, :, 0] = 0x5A5A5A5
+        for flags in (0, 1, 2, 3):
+            got = host(lbg.search(dev(d.view(np.int32), cuda), dev(d.view(np.int32), cuda), flags, 1,
+                                  bits=32 * nw - 2))
+            assert_same(got, oracle.search(d, d, flags, 1), f"nw={nw} flags={flags}")
+        d1 = d.copy()
+        d1[:, 4095, 0] ^= 1
+        q = d.copy()
+        q[:, :, 0] ^= 1
+        for flags in (0, 1):
+            got = host(lbg.search(dev(q.view(np.int32), cuda), dev(d1.view(np.int32), cuda), flags, 1,
+                                  bits=32 * nw - 2))
+            assert_same(got, oracle.search(q, d1, flags, 1), f"nw={nw} flags={flags} far best")
+
+
+def test_search_bits_rejected(cuda):
+    d = dev(np.zeros((1, 8, 1), np.int32), cuda)
+    for bits in (0, 33, -1):
+        with pytest.raises(ValueError, match="bit count"):
+            lbg.search(d, d, 0, bits=bits)
+
+
 def test_search_golden(cuda):
     z = golden("search.npz")
     for c in sorted({k.split("_")[0] for k in z.files}):
