@@ -496,8 +496,11 @@ __device__ bool infer_tile(InferSmem& S, const float (&x)[kIn], uint32_t phase, 
         mma_commit(mbar);
     }
     const bool ok = wait_or_abort(mbar, phase, &S.abort);
-    if (__syncthreads_or(!ok))
+    if (__syncthreads_or(!ok)) {
+        if (threadIdx.x == 0)  // the MMAs land before the TMEM is freed
+            wait_drain(mbar, phase);
         return false;
+    }
     fence_after();
     // layer 2 epilogue, two units per packed step; even and odd units
     // accumulate in the two lanes

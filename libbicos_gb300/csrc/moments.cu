@@ -364,6 +364,8 @@ __global__ void __launch_bounds__(kRowsM) k_moments(const __grid_constant__ Mome
         }
     }
 
+    if (tid == 0 && sh.abort)  // the MMAs land before the TMEM is freed
+        wait_drain(smem_u32(&sh.mbar), 0);
     fence_before();
     __syncthreads();
     if (tid == 0 && sh.abort)

@@ -227,7 +227,8 @@ __device__ __forceinline__ void merge_pair(float& kA, float& kB, int pair, int& 
     kA = kB = -INFINITY;
 }
 
-// Warp roles of the pipelined CTA (one CTA = one row x 128 query pixels):
+// Warp roles of the pipelined CTA (one CTA = one row x 128 query pixels;
+// the MMA and producer waits back off between polls, the epilogue's do not):
 //   warps 0..7   epilogue: warp w reads TMEM lane quarter w%4, columns
 //                [64*(w/4), 64*(w/4)+64) of each accumulator
 //   warps 8..11  producers: thread p expands candidate row p of each tile
@@ -307,9 +308,9 @@ __global__ void __launch_bounds__(kThreadsTC, 2) k_search_tc(const uint32_t* __r
             int issued = -1;
             for (int t = 0; t < ntiles; ++t) {
                 const int b = t & 1, slot = t % STAGES;
-                if (!wait_or_abort(smem_u32(&sh.full_b[slot]), (t / STAGES) & 1, abort))
+                if (!wait_or_abort<32>(smem_u32(&sh.full_b[slot]), (t / STAGES) & 1, abort))
                     break;
-                if (t >= 2 && !wait_or_abort(smem_u32(&sh.acc_empty[b]), ((t >> 1) - 1) & 1, abort))
+                if (t >= 2 && !wait_or_abort<32>(smem_u32(&sh.acc_empty[b]), ((t >> 1) - 1) & 1, abort))
                     break;
                 fence_after();
                 const uint32_t b_addr = smem_u32(sB + slot * TILE);
@@ -323,7 +324,7 @@ __global__ void __launch_bounds__(kThreadsTC, 2) k_search_tc(const uint32_t* __r
                 issued = t;
             }
             if (issued >= 0 && *abort)  // let the last MMA land before TMEM is freed
-                wait_or_abort(smem_u32(&sh.acc_full[issued & 1]), (issued >> 1) & 1, abort);
+                wait_drain(smem_u32(&sh.acc_full[issued & 1]), (issued >> 1) & 1);
         }
     } else if (warp >= kEpiWarps) {
         // ---- producers ----
@@ -349,7 +350,7 @@ __global__ void __launch_bounds__(kThreadsTC, 2) k_search_tc(const uint32_t* __r
                 const Desc<NW> cur = ring[i];
                 ring[i] = cand(t + PF);
                 const int slot = t % STAGES;
-                if (t >= STAGES && !wait_or_abort(smem_u32(&sh.b_empty[slot]), (t / STAGES - 1) & 1, abort)) {
+                if (t >= STAGES && !wait_or_abort<64>(smem_u32(&sh.b_empty[slot]), (t / STAGES - 1) & 1, abort)) {
                     live = false;
                     break;
                 }

@@ -54,7 +54,10 @@ __device__ __forceinline__ void mbar_arrive(uint32_t addr) {
 constexpr long long kWaitCycles = 4LL << 30;
 
 // bounded wait: false (and *abort set) when the phase does not complete in
-// time, or false at once when another thread already gave up
+// time, or false at once when another thread already gave up.  BACKOFF_NS
+// > 0 sleeps between polls (for waiters off the critical path, whose
+// polling would take issue slots from the warps doing the work).
+template<int BACKOFF_NS = 0>
 __device__ __forceinline__ bool wait_or_abort(uint32_t addr, uint32_t parity, volatile int* abort) {
     const long long start = clock64();
     while (!mbar_try_wait(addr, parity)) {
@@ -64,8 +67,18 @@ __device__ __forceinline__ bool wait_or_abort(uint32_t addr, uint32_t parity, vo
             *abort = 1;
             return false;
         }
+        if constexpr (BACKOFF_NS > 0)
+            __nanosleep(BACKOFF_NS);
     }
     return true;
+}
+
+// bounded wait that ignores the abort flag: an aborting CTA lets the MMAs
+// it issued land before it frees its TMEM
+__device__ __forceinline__ void wait_drain(uint32_t addr, uint32_t parity) {
+    const long long start = clock64();
+    while (!mbar_try_wait(addr, parity) && clock64() - start < kWaitCycles) {
+    }
 }
 
 // Shared-memory matrix descriptor, canonical K-major layout without
