@@ -47,7 +47,8 @@ enum {
     BICOS_16U = 2,
     BICOS_16S = 3,
     BICOS_32F = 5,
-    BICOS_64F = 6
+    BICOS_64F = 6,
+    BICOS_32FC3 = 21 /* three float channels per pixel (point clouds) */
 };
 
 typedef enum bicos_status {
@@ -212,6 +213,30 @@ bicos_status bicos_search_noalloc_v1(const uint32_t* desc0, const uint32_t* desc
                                      int32_t cols, uint32_t nwords, int32_t flags,
                                      int32_t max_lr_diff, bicos_image* disparity,
                                      bicos_stream_t stream);
+
+/*
+ * Point cloud of a disparity map: cv::reprojectImageTo3D(disparity, points,
+ * Q, false, CV_32F) as bicos-cli runs it after the match (src/cli.cpp:
+ * 228-250).  Every pixel (x, y) with disparity d becomes
+ * (X/W, Y/W, Z/W) with [X Y Z W]^T = Q [x y d 1]^T (W = 0 gives (0, 0, 0));
+ * invalid disparities are reprojected too, as values (INT16_MIN; NaN
+ * propagates) and left for the point-cloud writer to skip.
+ *   disparity  BICOS_16S or BICOS_32F device image (the match's output)
+ *   q          16 doubles, Q row-major (host memory, read during the call)
+ *   points     BICOS_32FC3 device image of the disparity's size
+ * Arithmetic in FP32 (fused sums of the Q terms).
+ */
+bicos_status bicos_reproject_v1(const bicos_image* disparity, const double* q, bicos_image* points,
+                                bicos_stream_t stream);
+
+/* Host utility of the command-line front end (no GPU work): reconstructs
+ * `height` PNG scanlines of `stride` bytes from the inflated image data
+ * `raw` (each row: one filter byte, then stride bytes; ISO/IEC 15948
+ * section 9) into `out`; bpp = bytes per complete pixel (at least 1).
+ * Returns 0, -1 for bad arguments, or r + 1 when row r names an unknown
+ * filter.  Replaces the PNG decoding libBICOS's CLI gets from
+ * cv::imread (src/fileutils.cpp:61-83). */
+int32_t bicos_png_unfilter(uint8_t* out, const uint8_t* raw, int32_t height, size_t stride, int32_t bpp);
 
 /* NCC agreement in place on an int16 disparity; min_var is the per-stack
  * threshold (min_variance * n) used when has_min_var is set. */

@@ -127,6 +127,23 @@ def search(desc0, desc1, flags: int, max_lr_diff: int = -1, stream=None, bits=No
     return out
 
 
+def reproject(disparity, q, out=None, stream=None):
+    """Point cloud of a disparity map (bicos_reproject_v1; bicos-cli's
+    cv::reprojectImageTo3D(disp, points, Q, false, CV_32F) step,
+    src/cli.cpp:228-250): a (rows, cols, 3) float32 CUDA tensor of
+    (X/W, Y/W, Z/W), [X Y Z W] = Q [x y d 1].  disparity: int16 or float32
+    CUDA tensor; q: 4x4 array-like."""
+    import numpy as np
+    import torch
+    qa = np.ascontiguousarray(np.asarray(q, dtype=np.float64).reshape(4, 4))
+    if out is None:
+        out = torch.empty((disparity.shape[0], disparity.shape[1], 3), dtype=torch.float32, device=disparity.device)
+    di, pi = N.tensor_image(disparity), N.points_image(out)
+    _raise(N.load().bicos_reproject_v1(C.byref(di), qa.ctypes.data_as(C.POINTER(C.c_double)), C.byref(pi),
+                                       _stream_ptr(stream)))
+    return out
+
+
 def agree(disp, stack0, stack1, threshold: float, min_var=None, double=False, stream=None):
     """In-place NCC agreement on an int16 disparity; returns (disp, corrmap).
     min_var is the per-stack value (min_variance * n)."""

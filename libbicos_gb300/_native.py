@@ -87,6 +87,8 @@ def load():
         "bicos_descriptor_transform_v1": ([IMG, U, I, U, P, P], C.c_int),
         "bicos_search_v1": ([P, P, I, I, U, I, I, IMG, P], C.c_int),
         "bicos_search_bits_v1": ([P, P, I, I, U, I, I, I, IMG, P], C.c_int),
+        "bicos_reproject_v1": ([IMG, C.POINTER(C.c_double), IMG, P], C.c_int),
+        "bicos_png_unfilter": ([P, P, C.c_int32, S, C.c_int32], C.c_int32),
         "bicos_search_noalloc_v1": ([P, P, I, I, U, I, I, IMG, P], C.c_int),
         "bicos_agree_v1": ([IMG, IMG, IMG, U, F, I, F, I, IMG, P], C.c_int),
         "bicos_agree_subpixel_v1": ([IMG, IMG, IMG, U, F, F, I, F, I, IMG, IMG, P], C.c_int),
@@ -142,6 +144,17 @@ def tensor_image(t) -> Image:
     if t.dim() != 2 or t.stride(1) != 1:
         raise ValueError("expected a 2-D tensor with unit column stride")
     return image(t.data_ptr(), t.shape[0], t.shape[1], type_of(t.dtype), t.stride(0) * t.element_size())
+
+
+TYPE_32FC3 = 21
+
+
+def points_image(t) -> Image:
+    """bicos_image view of a (rows, cols, 3) float32 CUDA tensor (packed
+    pixels, any row pitch)."""
+    if t.dim() != 3 or t.shape[2] != 3 or t.stride(2) != 1 or t.stride(1) != 3 or str(t.dtype) != "torch.float32":
+        raise ValueError("expected a (rows, cols, 3) float32 tensor with packed pixels")
+    return image(t.data_ptr(), t.shape[0], t.shape[1], TYPE_32FC3, t.stride(0) * 4)
 
 
 def image_array(images) -> C.Array:

@@ -143,6 +143,7 @@ int elem_bytes_of(int type) {
         case BICOS_16S: return 2;
         case BICOS_32F: return 4;
         case BICOS_64F: return 8;
+        case BICOS_32FC3: return 12;
         default: return 0;
     }
 }
@@ -905,6 +906,35 @@ bicos_status bicos_agree_learned_v1(const bicos_image* raw_disparity, const bico
         e = er;
     if (e != cudaSuccess)
         return cuda_fail(e, "learned agree launch");
+    return BICOS_OK;
+}
+
+bicos_status bicos_reproject_v1(const bicos_image* disparity, const double* q, bicos_image* points,
+                                bicos_stream_t stream) {
+    if (!disparity || !q || !points)
+        return fail(BICOS_ERR_INVALID_ARGUMENT, "null argument");
+    if (disparity->type != BICOS_16S && disparity->type != BICOS_32F)
+        return fail(BICOS_ERR_EXCEPTION, "disparity must be an int16 or float32 image");
+    if (disparity->rows < 1 || disparity->cols < 1 || !image_ok(disparity, disparity->rows, disparity->cols,
+                                                               disparity->type))
+        return fail(BICOS_ERR_EXCEPTION, "bad disparity image");
+    if (!image_ok(points, disparity->rows, disparity->cols, BICOS_32FC3))
+        return fail(BICOS_ERR_EXCEPTION, "points must be a three-channel float32 image of the disparity's size");
+    ReprojectParams p;
+    p.disp = disparity->data;
+    p.disp_pitch = (long long)disparity->step;
+    p.pts = static_cast<float*>(points->data);
+    p.pts_pitch = (long long)points->step;
+    p.rows = disparity->rows;
+    p.cols = disparity->cols;
+    for (int i = 0; i < 16; ++i) {
+        if (!std::isfinite(q[i]))
+            return fail(BICOS_ERR_INVALID_ARGUMENT, "Q must be finite");
+        p.q[i] = (float)q[i];
+    }
+    cudaError_t e = launch_reproject(p, disparity->type == BICOS_32F, reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess)
+        return cuda_fail(e, "reprojection launch");
     return BICOS_OK;
 }
 

@@ -71,6 +71,17 @@ cudaError_t launch_search(const uint32_t* desc0, const uint32_t* desc1, int rows
                           long long disp_pitch, int32_t* best0, int32_t* best1,
                           cudaStream_t st);
 
+// point-cloud reprojection (reproject.cu): q = Q row-major, as floats
+struct ReprojectParams {
+    const void* disp;
+    long long disp_pitch;
+    float* pts;
+    long long pts_pitch;
+    int rows, cols;
+    float q[16];
+};
+cudaError_t launch_reproject(const ReprojectParams& p, bool float_disp, cudaStream_t st);
+
 // tensor-core search (search_tc.cu): same contract as launch_search, for
 // rows of at most 4096 columns
 bool search_tc_supported(int cols);
