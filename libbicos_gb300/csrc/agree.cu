@@ -309,11 +309,17 @@ __global__ void __launch_bounds__(kListThreads) k_subpixel_list(const __grid_con
 constexpr int kSubThreads = 64;
 
 // Packed FP32 pairs (sm_100+ f32x2 arithmetic): two sweep positions per
-// instruction, each lane rounded like the scalar operation.  Used only where
-// no multiply feeds an add (rounding, sums) or where the reference itself
-// fuses (the FMAs of the second pass): a packed multiply-add chain is not
-// guaranteed to keep the reference's separate roundings, so the interpolant
-// stays scalar.
+// instruction, each lane rounded like the scalar operation (checked one
+// operation at a time against the scalar IEEE intrinsics).  A packed
+// multiply whose result feeds a packed add is not kept as two roundings by
+// the code generator (add.rn/mul.rn notwithstanding; about 40 % of random
+// cases came out fused), and neither is fma(t, 1, u) with a literal 1 (it
+// is folded into fma(p, q, u) when t = p * q).  So every sum whose operand
+// is a product is an explicit fma(t, one, u) with `one` a kernel parameter
+// (AgreeParams::one = 1): exact (t * 1 = t) and opaque to the code
+// generator.  The interpolant ((a*x)*x + b*x) + c is then three packed
+// multiplies and two such FMAs per pair of positions, bit for bit the
+// reference's five roundings.
 typedef unsigned long long f2;
 __device__ __forceinline__ f2 pk(float lo, float hi) {
     f2 r;
@@ -337,6 +343,17 @@ __device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
     f2 r;
     asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
     return r;
+}
+__device__ __forceinline__ f2 mul2(f2 a, f2 b) {
+    f2 r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+// ((a*x)*x + b*x) + c on both lanes with the reference's five roundings;
+// one = {1, 1} from a kernel parameter
+__device__ __forceinline__ f2 interp2(float a, float b, float c, f2 x, f2 one) {
+    const f2 t = fma2(mul2(mul2(pk(a, a), x), x), one, mul2(pk(b, b), x));
+    return fma2(t, one, pk(c, c));
 }
 // round_wrap_f on both lanes
 template<typename T>
@@ -409,6 +426,7 @@ __device__ __forceinline__ void subpixel_f32_body(const AgreeParams& p, int bx, 
             }
             float best_x = 0.f, best = -1.f;
             float xs = -1.f;
+            const f2 one2 = pk(p.one, p.one);
             while (xs <= 1.f) {
                 float xv[XG];
                 bool on[XG];
@@ -420,23 +438,19 @@ __device__ __forceinline__ void subpixel_f32_body(const AgreeParams& p, int bx, 
                 }
                 constexpr int XP = XG / 2;  // position pairs
                 f2 iv[XP][NMAX];
-                f2 s1[XP];
+                f2 s1[XP], xq[XP];
 #pragma unroll
-                for (int q = 0; q < XP; ++q)
+                for (int q = 0; q < XP; ++q) {
                     s1[q] = 0ull;
+                    xq[q] = pk(xv[2 * q], xv[2 * q + 1]);
+                }
 #pragma unroll
                 for (int t = 0; t < NMAX; ++t) {
                     if (t < n) {
                         const float4 k = coef[t * kSubThreads + tid];
 #pragma unroll
                         for (int q = 0; q < XP; ++q) {
-                            float v[2];
-#pragma unroll
-                            for (int h = 0; h < 2; ++h) {
-                                const float x = xv[2 * q + h];
-                                v[h] = __fadd_rn(__fadd_rn(__fmul_rn(__fmul_rn(k.x, x), x), __fmul_rn(k.y, x)), k.z);
-                            }
-                            iv[q][t] = round_wrap2<T>(pk(v[0], v[1]));
+                            iv[q][t] = round_wrap2<T>(interp2(k.x, k.y, k.z, xq[q], one2));
                             s1[q] = add2(s1[q], iv[q][t]);
                         }
                     }

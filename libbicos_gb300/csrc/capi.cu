@@ -367,6 +367,7 @@ cudaError_t bicos_gb300::enqueue_search(const MatchPlan& P, const MatchBuffers& 
 AgreeParams bicos_gb300::agree_params(const MatchPlan& P, const MatchBuffers& m) {
     AgreeParams ap;
     std::memset(&ap, 0, sizeof ap);
+    ap.one = 1.0f;
     ap.s = P.s;
     ap.thr = P.cfg->nxcorr_threshold;
     ap.step = P.sub ? P.cfg->subpixel_step : -1.f;
@@ -771,6 +772,7 @@ bicos_status bicos_agree_v1(bicos_image* disparity, const bicos_image* stack0, c
         return fail(BICOS_ERR_EXCEPTION, "corrmap type or size mismatch");
     AgreeParams ap;
     std::memset(&ap, 0, sizeof ap);
+    ap.one = 1.0f;
     fill_stack(ap.s, stack0, stack1, n, eb);
     ap.raw_io = static_cast<int16_t*>(disparity->data);
     ap.raw_pitch = (long long)disparity->step;
@@ -806,6 +808,7 @@ bicos_status bicos_agree_subpixel_v1(const bicos_image* raw_disparity, const bic
         return fail(BICOS_ERR_EXCEPTION, "corrmap type or size mismatch");
     AgreeParams ap;
     std::memset(&ap, 0, sizeof ap);
+    ap.one = 1.0f;
     fill_stack(ap.s, stack0, stack1, n, eb);
     ap.raw = static_cast<const int16_t*>(raw_disparity->data);
     ap.raw_pitch = (long long)raw_disparity->step;
@@ -883,6 +886,7 @@ bicos_status bicos_agree_learned_v1(const bicos_image* raw_disparity, const bico
         return fail(BICOS_ERR_INVALID_ARGUMENT, err);
     AgreeParams ap;
     std::memset(&ap, 0, sizeof ap);
+    ap.one = 1.0f;
     fill_stack(ap.s, stack0, stack1, n, eb);
     ap.raw = static_cast<const int16_t*>(raw_disparity->data);
     ap.raw_pitch = (long long)raw_disparity->step;

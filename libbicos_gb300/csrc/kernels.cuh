@@ -37,6 +37,9 @@ struct AgreeParams {
     float step;
     int has_minvar;
     float minvar;
+    // 1.0, read at run time: the sweep's packed sums fma(t, one, u) must not
+    // be folded with the product that made t, which a literal 1 would allow
+    float one = 1.0f;
 };
 
 // moment form of the NCC stage (moments.cu)
