@@ -388,41 +388,69 @@ __device__ __forceinline__ void subpixel_f32_body(const AgreeParams& p, int bx, 
     const bool mv = p.has_minvar != 0;
     const float fn = (float)n;
     if (d != kInvalidDisp && col1 >= 0 && col1 < cols) {
-        // two streaming passes over the frames (sums, then centred values)
-        int sx = 0, sy = 0;
         const bool border = col1 == 0 || col1 == cols - 1;
-#pragma unroll 4
-        for (int t = 0; t < n; ++t) {
-            sx += ld_px<T>(p.s, 0, t, row, col);
-            if (border)
-                sy += ld_px<T>(p.s, 1, t, row, col1);
+        // up to 33 frames, every sample of the pixel is requested at once
+        // (the left column and the right triplet of each frame; the border
+        // case reads the right column only), so the staging pays one memory
+        // latency, not one per few frames; larger stacks (which would not
+        // fit in registers) stream the frames, four at a time
+        constexpr bool kAll = NMAX <= 33;
+        constexpr int NR = kAll ? NMAX : 1;
+        int xl[NR], yl[NR], yc[NR], yr[NR];
+        auto sample = [&](int side, int t, int c) { return ld_px<T>(p.s, side, t, row, c); };
+        if constexpr (kAll) {
+#pragma unroll
+            for (int t = 0; t < NMAX; ++t) {
+                if (t < n) {
+                    xl[t] = sample(0, t, col);
+                    yc[t] = sample(1, t, col1);
+                    if (!border) {
+                        yl[t] = sample(1, t, col1 - 1);
+                        yr[t] = sample(1, t, col1 + 1);
+                    }
+                }
+            }
         }
+        auto X = [&](int t) { return kAll ? xl[kAll ? t : 0] : sample(0, t, col); };
+        auto YL = [&](int t) { return kAll ? yl[kAll ? t : 0] : sample(1, t, col1 - 1); };
+        auto YC = [&](int t) { return kAll ? yc[kAll ? t : 0] : sample(1, t, col1); };
+        auto YR = [&](int t) { return kAll ? yr[kAll ? t : 0] : sample(1, t, col1 + 1); };
+        int sx = 0, sy = 0;
+#pragma unroll
+        for (int t = 0; t < NMAX; ++t)
+            if (t < n) {
+                sx += X(t);
+                if (kAll || border)
+                    sy += YC(t);
+            }
         const float m0 = __fdiv_rn((float)sx, fn);
         if (border) {
             const float m1 = __fdiv_rn((float)sy, fn);
             float cov = 0.f, var0 = 0.f, var1 = 0.f;
-#pragma unroll 4
-            for (int t = 0; t < n; ++t) {
-                const float d0 = __fsub_rn((float)ld_px<T>(p.s, 0, t, row, col), m0);
-                const float d1 = __fsub_rn((float)ld_px<T>(p.s, 1, t, row, col1), m1);
-                cov = __fmaf_rn(d0, d1, cov);
-                var0 = __fmaf_rn(d0, d0, var0);
-                var1 = __fmaf_rn(d1, d1, var1);
+#pragma unroll
+            for (int t = 0; t < NMAX; ++t) {
+                if (t < n) {
+                    const float d0 = __fsub_rn((float)X(t), m0);
+                    const float d1 = __fsub_rn((float)YC(t), m1);
+                    cov = __fmaf_rn(d0, d1, cov);
+                    var0 = __fmaf_rn(d0, d0, var0);
+                    var1 = __fmaf_rn(d1, d1, var1);
+                }
             }
             corr = nxc_from(cov, var0, var1, mv, p.minvar);
             if (!(corr < p.thr))
                 result = (float)d;
         } else {
             float var0 = 0.f;
-#pragma unroll 4
-            for (int t = 0; t < n; ++t) {
-                const float d0 = __fsub_rn((float)ld_px<T>(p.s, 0, t, row, col), m0);
-                var0 = __fmaf_rn(d0, d0, var0);
-                const int y0 = ld_px<T>(p.s, 1, t, row, col1 - 1);
-                const int y1 = ld_px<T>(p.s, 1, t, row, col1);
-                const int y2 = ld_px<T>(p.s, 1, t, row, col1 + 1);
-                coef[t * kSubThreads + tid] =
-                    make_float4(0.5f * (float)(y0 - 2 * y1 + y2), 0.5f * (float)(y2 - y0), (float)y1, d0);
+#pragma unroll
+            for (int t = 0; t < NMAX; ++t) {
+                if (t < n) {
+                    const float d0 = __fsub_rn((float)X(t), m0);
+                    var0 = __fmaf_rn(d0, d0, var0);
+                    const int y0 = YL(t), y1 = YC(t), y2 = YR(t);
+                    coef[t * kSubThreads + tid] =
+                        make_float4(0.5f * (float)(y0 - 2 * y1 + y2), 0.5f * (float)(y2 - y0), (float)y1, d0);
+                }
             }
             float best_x = 0.f, best = -1.f;
             float xs = -1.f;
