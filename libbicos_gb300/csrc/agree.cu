@@ -600,39 +600,69 @@ __device__ __forceinline__ void subpixel_f64_body(const AgreeParams& p, int bx, 
     if (d != kInvalidDisp && col1 >= 0 && col1 < cols) {
         long long sx = 0, sxx = 0, sy = 0;
         const bool border = col1 == 0 || col1 == cols - 1;
-        for (int t = 0; t < n; ++t) {
-            const int x = ld_px<T>(p.s, 0, t, row, col);
-            sx += x;
-            sxx += (long long)x * x;
-            if (border)
-                sy += ld_px<T>(p.s, 1, t, row, col1);
+        // up to 33 frames every sample is requested at once, as in the
+        // single-precision sweep; larger stacks stream the frames
+        constexpr bool kAll = NMAX <= 33;
+        constexpr int NR = kAll ? NMAX : 1;
+        int xl[NR], yl[NR], yc[NR], yr[NR];
+        auto sample = [&](int side, int t, int c) { return ld_px<T>(p.s, side, t, row, c); };
+        if constexpr (kAll) {
+#pragma unroll
+            for (int t = 0; t < NMAX; ++t) {
+                if (t < n) {
+                    xl[t] = sample(0, t, col);
+                    yc[t] = sample(1, t, col1);
+                    if (!border) {
+                        yl[t] = sample(1, t, col1 - 1);
+                        yr[t] = sample(1, t, col1 + 1);
+                    }
+                }
+            }
+        }
+        auto X = [&](int t) { return kAll ? xl[kAll ? t : 0] : sample(0, t, col); };
+        auto YL = [&](int t) { return kAll ? yl[kAll ? t : 0] : sample(1, t, col1 - 1); };
+        auto YC = [&](int t) { return kAll ? yc[kAll ? t : 0] : sample(1, t, col1); };
+        auto YR = [&](int t) { return kAll ? yr[kAll ? t : 0] : sample(1, t, col1 + 1); };
+#pragma unroll
+        for (int t = 0; t < NMAX; ++t) {
+            if (t < n) {
+                const int x = X(t);
+                sx += x;
+                sxx += (long long)x * x;
+                if (border)
+                    sy += YC(t);
+            }
         }
         const double m0 = __ddiv_rn((double)sx, dn);
         if (border) {
             const double m1 = __ddiv_rn((double)sy, dn);
             double cov = 0.0, var0 = 0.0, var1 = 0.0;
-            for (int t = 0; t < n; ++t) {
-                const double d0 = __dsub_rn((double)ld_px<T>(p.s, 0, t, row, col), m0);
-                const double d1 = __dsub_rn((double)ld_px<T>(p.s, 1, t, row, col1), m1);
-                cov = __fma_rn(d0, d1, cov);
-                var0 = __fma_rn(d0, d0, var0);
-                var1 = __fma_rn(d1, d1, var1);
+#pragma unroll
+            for (int t = 0; t < NMAX; ++t) {
+                if (t < n) {
+                    const double d0 = __dsub_rn((double)X(t), m0);
+                    const double d1 = __dsub_rn((double)YC(t), m1);
+                    cov = __fma_rn(d0, d1, cov);
+                    var0 = __fma_rn(d0, d0, var0);
+                    var1 = __fma_rn(d1, d1, var1);
+                }
             }
             corr = (mv && (var0 < minvar || var1 < minvar)) ? -1.0 : __ddiv_rn(cov, __dsqrt_rn(__dmul_rn(var0, var1)));
             if (!(corr < (double)p.thr))
                 result = (float)d;
         } else {
             double var0 = 0.0;
-            for (int t = 0; t < n; ++t) {
-                const int x = ld_px<T>(p.s, 0, t, row, col);
-                const double d0 = __dsub_rn((double)x, m0);
-                var0 = __fma_rn(d0, d0, var0);
-                const int y0 = ld_px<T>(p.s, 1, t, row, col1 - 1);
-                const int y1 = ld_px<T>(p.s, 1, t, row, col1);
-                const int y2 = ld_px<T>(p.s, 1, t, row, col1 + 1);
-                coef[t * kSubThreads + tid] =
-                    make_float4(0.5f * (float)(y0 - 2 * y1 + y2), 0.5f * (float)(y2 - y0), (float)y1,
-                                __int_as_float(x));
+#pragma unroll
+            for (int t = 0; t < NMAX; ++t) {
+                if (t < n) {
+                    const int x = X(t);
+                    const double d0 = __dsub_rn((double)x, m0);
+                    var0 = __fma_rn(d0, d0, var0);
+                    const int y0 = YL(t), y1 = YC(t), y2 = YR(t);
+                    coef[t * kSubThreads + tid] =
+                        make_float4(0.5f * (float)(y0 - 2 * y1 + y2), 0.5f * (float)(y2 - y0), (float)y1,
+                                    __int_as_float(x));
+                }
             }
             // exact left moment and its min-variance decision
             const long long dx = (long long)n * sxx - sx * sx;  // n^2 * variance
