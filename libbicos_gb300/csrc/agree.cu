@@ -376,7 +376,14 @@ __device__ __forceinline__ float nxc_from(float cov, float var0, float var1, boo
 template<typename T, int NMAX>
 __device__ __forceinline__ void subpixel_f32_body(const AgreeParams& p, int bx, int row) {
     constexpr int XG = NMAX <= 33 ? 4 : 2;
-    extern __shared__ float4 coef[];  // [NMAX][kSubThreads]: a, b, c, d0
+    // staged per frame and pixel, as planes: (a, b) pairs, c, d0 (each
+    // plane [NMAX][kSubThreads]; 16 bytes per frame and pixel in all) --
+    // a thread's reads are consecutive across the warp in every plane, so
+    // none conflicts
+    extern __shared__ float4 coef_raw[];
+    float2* const cab = reinterpret_cast<float2*>(coef_raw);
+    float* const cc = reinterpret_cast<float*>(cab + NMAX * kSubThreads);
+    float* const cd0 = cc + NMAX * kSubThreads;
     const int tid = threadIdx.x;
     const int col = bx * kSubThreads + tid;
     const int cols = p.s.cols, n = p.s.n;
@@ -448,8 +455,9 @@ __device__ __forceinline__ void subpixel_f32_body(const AgreeParams& p, int bx, 
                     const float d0 = __fsub_rn((float)X(t), m0);
                     var0 = __fmaf_rn(d0, d0, var0);
                     const int y0 = YL(t), y1 = YC(t), y2 = YR(t);
-                    coef[t * kSubThreads + tid] =
-                        make_float4(0.5f * (float)(y0 - 2 * y1 + y2), 0.5f * (float)(y2 - y0), (float)y1, d0);
+                    cab[t * kSubThreads + tid] = make_float2(0.5f * (float)(y0 - 2 * y1 + y2), 0.5f * (float)(y2 - y0));
+                    cc[t * kSubThreads + tid] = (float)y1;
+                    cd0[t * kSubThreads + tid] = d0;
                 }
             }
             float best_x = 0.f, best = -1.f;
@@ -475,10 +483,11 @@ __device__ __forceinline__ void subpixel_f32_body(const AgreeParams& p, int bx, 
 #pragma unroll
                 for (int t = 0; t < NMAX; ++t) {
                     if (t < n) {
-                        const float4 k = coef[t * kSubThreads + tid];
+                        const float2 ab = cab[t * kSubThreads + tid];
+                        const float c = cc[t * kSubThreads + tid];
 #pragma unroll
                         for (int q = 0; q < XP; ++q) {
-                            iv[q][t] = round_wrap2<T>(interp2(k.x, k.y, k.z, xq[q], one2));
+                            iv[q][t] = round_wrap2<T>(interp2(ab.x, ab.y, c, xq[q], one2));
                             s1[q] = add2(s1[q], iv[q][t]);
                         }
                     }
@@ -495,7 +504,7 @@ __device__ __forceinline__ void subpixel_f32_body(const AgreeParams& p, int bx, 
 #pragma unroll
                 for (int t = 0; t < NMAX; ++t) {
                     if (t < n) {
-                        const float d0 = coef[t * kSubThreads + tid].w;
+                        const float d0 = cd0[t * kSubThreads + tid];
                         const f2 D0 = pk(d0, d0);
 #pragma unroll
                         for (int q = 0; q < XP; ++q) {
