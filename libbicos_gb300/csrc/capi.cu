@@ -608,15 +608,22 @@ bicos_status bicos_match_host_v1(const void* const* frames0, const void* const* 
     };
     const long long sp0 = spacing(frames0), sp1 = spacing(frames1);
     const bool dense = host_step == row_bytes;
+    // large stacks: a short first band (its upload is the one that nothing
+    // hides), then three equal bands
     const int bands = (size_t)rows * cols * n >= ((size_t)32 << 20) && rows >= 64 ? 4 : 1;
-    const int band_rows = (rows + bands - 1) / bands;
+    auto band_start = [&](int k) -> int {
+        if (bands == 1)
+            return k == 0 ? 0 : rows;
+        const int first = rows / 10;
+        return k == 0 ? 0 : first + (int)((long long)(rows - first) * (k - 1) / (bands - 1));
+    };
 
     cudaError_t e = cudaEventRecord(hp.fork, st);
     if (e == cudaSuccess)
         e = cudaStreamWaitEvent(hp.side, hp.fork, 0);
     bicos_status rs = BICOS_OK;
     for (int k = 0; k < bands && e == cudaSuccess && rs == BICOS_OK; ++k) {
-        const int r0 = k * band_rows, nr = std::min(band_rows, rows - r0);
+        const int r0 = band_start(k), nr = band_start(k + 1) - r0;
         if (nr <= 0)
             break;
         cudaStream_t bs = (k & 1) ? hp.side : st;
