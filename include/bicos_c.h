@@ -20,6 +20,13 @@
  *                                  include/impl/cuda/agree.cuh:161-259
  *   bicos_config_default           BICOS::Config defaults, include/common.hpp:73-82
  *   bicos_last_error               BICOS::Exception::what(), src/exception.cpp:23-27
+ *   bicos_reproject_v1             bicos-cli's cv::reprojectImageTo3D step,
+ *                                  src/cli.cpp:228-250
+ *   bicos_png_unfilter             the PNG decoding bicos-cli gets from cv::imread,
+ *                                  src/fileutils.cpp:61-83 (host utility)
+ * Extensions without a reference counterpart: bicos_match_host_v1 (host
+ * buffers, pybicos's path), bicos_search_bits_v1, bicos_search_noalloc_v1,
+ * the learned-form, MLP and batch entry points.
  *
  * Error behaviour: every entry point returns a bicos_status.  Messages match
  * the reference's exception texts ("need at least two images", "bad input
