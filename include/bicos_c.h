@@ -245,6 +245,25 @@ bicos_status bicos_reproject_v1(const bicos_image* disparity, const double* q, b
  * cv::imread (src/fileutils.cpp:61-83). */
 int32_t bicos_png_unfilter(uint8_t* out, const uint8_t* raw, int32_t height, size_t stride, int32_t bpp);
 
+/*
+ * Frame-by-frame ingest (no counterpart in the reference, whose CLI uploads
+ * finished stacks, src/cli.cpp:177-183): a handle owns the device frames of
+ * one stack shape.  Each push uploads frame t (0 <= t < n) of both sides
+ * from host memory (row step host_step) on `stream` -- asynchronous for
+ * pinned memory, so uploads overlap the capture of the next patterns; the
+ * host buffers must stay valid until the copy has run.  Pushing a frame
+ * again replaces it.  The match runs bicos_match_v1 on the resident frames
+ * once every frame has been pushed (BICOS_ERR_EXCEPTION otherwise), ordered
+ * after all pushes, on `stream`; outputs as bicos_match_v1.
+ */
+typedef struct bicos_ingest bicos_ingest;
+bicos_status bicos_ingest_create(bicos_ingest** out, int32_t rows, int32_t cols, uint32_t n, int32_t type);
+bicos_status bicos_ingest_destroy(bicos_ingest* h);
+bicos_status bicos_ingest_push_v1(bicos_ingest* h, uint32_t t, const void* frame0, const void* frame1,
+                                  size_t host_step, bicos_stream_t stream);
+bicos_status bicos_ingest_match_v1(bicos_ingest* h, bicos_image* disparity, bicos_image* corrmap,
+                                   const bicos_config* cfg, bicos_stream_t stream);
+
 /* NCC agreement in place on an int16 disparity; min_var is the per-stack
  * threshold (min_variance * n) used when has_min_var is set. */
 bicos_status bicos_agree_v1(bicos_image* disparity, const bicos_image* stack0,

@@ -205,6 +205,79 @@ def agree_learned(raw, stack0, stack1, threshold: float, step: float, min_var=No
     return out, corr, prop, int(count.value)
 
 
+class Ingest:
+    """Frame-by-frame ingest (bicos_ingest_*): device frames for one stack
+    shape; push(t, left, right) uploads frame t of both sides as it arrives
+    (host numpy arrays or pinned torch CPU tensors, 2-D uint8/uint16), and
+    match(cfg) runs BICOS::match on the resident frames once all n were
+    pushed.  Pushed host buffers are referenced until they are replaced or
+    the handle is closed (pinned memory is copied asynchronously)."""
+
+    def __init__(self, rows: int, cols: int, n: int, dtype="uint8"):
+        self._lib = N.load()
+        self.rows, self.cols, self.n = rows, cols, n
+        self._type = N.BICOS_8U if str(dtype).endswith("uint8") else N.BICOS_16U
+        h = C.c_void_p()
+        _raise(self._lib.bicos_ingest_create(C.byref(h), rows, cols, n, self._type))
+        self._h = h
+        self._keep = {}
+
+    def close(self):
+        if self._h:
+            self._lib.bicos_ingest_destroy(self._h)
+            self._h = None
+        self._keep.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def _host(a):
+        if hasattr(a, "data_ptr"):  # torch CPU tensor
+            if a.dim() != 2 or a.stride(1) != 1:
+                raise ValueError("expected 2-D frames with unit column stride")
+            return a, a.data_ptr(), a.stride(0) * a.element_size()
+        import numpy as np
+        a = np.ascontiguousarray(a)
+        if a.ndim != 2:
+            raise ValueError("expected 2-D frames")
+        return a, a.ctypes.data, a.strides[0]
+
+    def push(self, t: int, left, right, stream=None):
+        l, lp, ls = self._host(left)
+        r, rp, rs = self._host(right)
+        if ls != rs:
+            raise ValueError("both frames must share the row step")
+        _raise(self._lib.bicos_ingest_push_v1(self._h, t, C.c_void_p(lp), C.c_void_p(rp), ls, _stream_ptr(stream)))
+        self._keep[t] = (l, r)
+
+    def match(self, cfg: Config | None = None, stream=None, out=None, corrmap=True):
+        """(disparity, corrmap or None) CUDA tensors, as match_device."""
+        import torch
+        cfg = Config() if cfg is None else cfg
+        nc = cfg.native()
+        dt, ct = C.c_int32(), C.c_int32()
+        N.check(self._lib.bicos_output_types(C.byref(nc), C.byref(dt), C.byref(ct)))
+        if out is not None:
+            disp, corr = out
+        else:
+            dev = torch.device("cuda")
+            disp = torch.empty((self.rows, self.cols), dtype=torch.int16 if dt.value == N.BICOS_16S else torch.float32,
+                               device=dev)
+            corr = None
+            if corrmap and ct.value >= 0:
+                corr = torch.empty((self.rows, self.cols),
+                                   dtype=torch.float64 if ct.value == N.BICOS_64F else torch.float32, device=dev)
+        di = N.tensor_image(disp)
+        ci = N.tensor_image(corr) if corr is not None else None
+        _raise(self._lib.bicos_ingest_match_v1(self._h, C.byref(di), C.byref(ci) if ci is not None else None,
+                                               C.byref(nc), _stream_ptr(stream)))
+        return disp, corr
+
+
 class Batch:
     """Many stacks per call (bicos_match_batch_v1): one CUDA graph per batch
     signature, persistent multi-stack launches, an autotuner over launch

@@ -89,6 +89,10 @@ def load():
         "bicos_search_bits_v1": ([P, P, I, I, U, I, I, I, IMG, P], C.c_int),
         "bicos_reproject_v1": ([IMG, C.POINTER(C.c_double), IMG, P], C.c_int),
         "bicos_png_unfilter": ([P, P, C.c_int32, S, C.c_int32], C.c_int32),
+        "bicos_ingest_create": ([C.POINTER(P), I, I, U, I], C.c_int),
+        "bicos_ingest_destroy": ([P], C.c_int),
+        "bicos_ingest_push_v1": ([P, U, P, P, S, P], C.c_int),
+        "bicos_ingest_match_v1": ([P, IMG, IMG, CFG, P], C.c_int),
         "bicos_search_noalloc_v1": ([P, P, I, I, U, I, I, IMG, P], C.c_int),
         "bicos_agree_v1": ([IMG, IMG, IMG, U, F, I, F, I, IMG, P], C.c_int),
         "bicos_agree_subpixel_v1": ([IMG, IMG, IMG, U, F, F, I, F, I, IMG, IMG, P], C.c_int),

@@ -129,3 +129,23 @@ def test_batch_handle_host_side(native):
     assert lib.bicos_match_batch_v1(h, None, 0, None) == native.OK  # empty batch: nothing to do
     assert lib.bicos_batch_captures(h) == 0
     assert lib.bicos_batch_destroy(h) == native.OK
+
+
+def test_ingest_handle_validation(native):
+    """bicos_ingest_create rejects bad stack shapes before any device work
+    (the reference's exception texts); null handles are rejected too."""
+    lib = native.load()
+    h = C.c_void_p()
+    cases = [((8, 8, 1, native.BICOS_8U), "need at least two images"),
+             ((8, 8, 66, native.BICOS_8U), "Bad number of images"),
+             ((8, 8, 4, native.BICOS_16S), "bad input depths"),
+             ((0, 8, 4, native.BICOS_8U), "empty images"),
+             ((8, 40000, 4, native.BICOS_8U), "int16 disparity range")]
+    for args, msg in cases:
+        assert lib.bicos_ingest_create(C.byref(h), *args) == native.ERR_EXCEPTION
+        assert msg in lib.bicos_last_error().decode()
+        assert not h.value
+    assert lib.bicos_ingest_create(None, 8, 8, 4, native.BICOS_8U) == native.ERR_INVALID_ARGUMENT
+    assert lib.bicos_ingest_destroy(None) == 0
+    assert lib.bicos_ingest_push_v1(None, 0, None, None, 8, None) == native.ERR_INVALID_ARGUMENT
+    assert lib.bicos_ingest_match_v1(None, None, None, None, None) == native.ERR_INVALID_ARGUMENT
