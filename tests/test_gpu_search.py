@@ -103,3 +103,17 @@ def test_search_single_column(cuda, oracle):
 def test_no_kernel_wait_ran_out(cuda, native):
     """the tensor-core search's bounded waits never expired in this process"""
     assert native.load().bicos_kernel_faults() == 0
+
+
+def test_search_known_answers(cuda):
+    """the hand-worked cases of tests/test_oracle_kat.py on the GPU, in the
+    plain and the column-coded form"""
+    from test_oracle_kat import _rows, INV
+    cases = [([3, 1, 1, 2, 4], 0, -1, [-1, 0, 1, 2, 3]), ([3, 1, 1, 2, 4], 1, -1, [INV] * 5),
+             ([2, 1, 3, 1, 0], 1, -1, [-4, -3, -2, -1, 0]), ([2, 1, 3, 1, 0], 2, 1, [-4, -4, INV, INV, INV]),
+             ([2, 1, 3, 1, 0], 2, 3, [-4, -4, -3, -3, INV]), ([2, 1, 3, 1, 0], 3, 3, [INV] * 5)]
+    for costs, flags, lr, want in cases:
+        d0, d1 = _rows(costs)
+        for bits in (None, 30):
+            got = host(lbg.search(dev(d0.view(np.int32), cuda), dev(d1.view(np.int32), cuda), flags, lr, bits=bits))
+            assert got.tolist() == [want], (costs, flags, lr, bits)

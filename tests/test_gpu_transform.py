@@ -43,3 +43,13 @@ def test_transform_pitched_frames(cuda, oracle):
     frames = [big[i, :, :100] for i in range(12)]
     got = host(lbg.descriptor_transform(frames, False))
     assert_same(got, oracle.transform(s, False, got.shape[-1]))
+
+
+def test_limited_known_answers(cuda):
+    """the hand-worked descriptors of tests/test_oracle_kat.py on the GPU"""
+    from test_oracle_kat import _transform_cases
+    for pix, want in _transform_cases():
+        n = len(pix)
+        stack = dev(np.array(pix, dtype=np.uint8).reshape(n, 1, 1), cuda)
+        d = host(lbg.descriptor_transform(stack, False))
+        assert int(d.reshape(-1)[0]) == want, pix
