@@ -373,7 +373,10 @@ __device__ __forceinline__ float nxc_from(float cov, float var0, float var1, boo
     return (mv && (var0 < minvar || var1 < minvar)) ? -1.f : __fdiv_rn(cov, __fsqrt_rn(__fmul_rn(var0, var1)));
 }
 
-template<typename T, int NMAX>
+// PREFETCH: request all of a pixel's samples at once (grid launches); the
+// persistent multi-stack form streams them, its claim loop leaving no
+// registers for the prefetch
+template<typename T, int NMAX, bool PREFETCH = true>
 __device__ __forceinline__ void subpixel_f32_body(const AgreeParams& p, int bx, int row) {
     constexpr int XG = NMAX <= 33 ? 4 : 2;
     // staged per frame and pixel, as planes: (a, b) pairs, c, d0 (each
@@ -401,7 +404,7 @@ __device__ __forceinline__ void subpixel_f32_body(const AgreeParams& p, int bx, 
         // case reads the right column only), so the staging pays one memory
         // latency, not one per few frames; larger stacks (which would not
         // fit in registers) stream the frames, four at a time
-        constexpr bool kAll = NMAX <= 33;
+        constexpr bool kAll = PREFETCH && NMAX <= 33;
         constexpr int NR = kAll ? NMAX : 1;
         int xl[NR], yl[NR], yc[NR], yr[NR];
         auto sample = [&](int side, int t, int c) { return ld_px<T>(p.s, side, t, row, c); };
@@ -423,13 +426,21 @@ __device__ __forceinline__ void subpixel_f32_body(const AgreeParams& p, int bx, 
         auto YC = [&](int t) { return kAll ? yc[kAll ? t : 0] : sample(1, t, col1); };
         auto YR = [&](int t) { return kAll ? yr[kAll ? t : 0] : sample(1, t, col1 + 1); };
         int sx = 0, sy = 0;
+        if constexpr (kAll) {
 #pragma unroll
-        for (int t = 0; t < NMAX; ++t)
-            if (t < n) {
+            for (int t = 0; t < NMAX; ++t)
+                if (t < n) {
+                    sx += X(t);
+                    sy += YC(t);
+                }
+        } else {
+#pragma unroll 4
+            for (int t = 0; t < n; ++t) {
                 sx += X(t);
-                if (kAll || border)
+                if (border)
                     sy += YC(t);
             }
+        }
         const float m0 = __fdiv_rn((float)sx, fn);
         if (border) {
             const float m1 = __fdiv_rn((float)sy, fn);
@@ -791,7 +802,7 @@ struct SubF32Op {
     static constexpr int kMaxThreads = kSubThreads;
     static constexpr int kMinBlocks = 1;
     static __device__ __forceinline__ void run(const P& p, int bx, int row, int) {
-        subpixel_f32_body<T, NMAX>(p, bx, row);
+        subpixel_f32_body<T, NMAX, false>(p, bx, row);
     }
 };
 template<typename T, int NMAX>
