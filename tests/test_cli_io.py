@@ -247,3 +247,28 @@ def test_reproject_oracle_conventions():
     f = np.array([[np.nan, 2.0]], np.float32)
     assert np.isnan(opc.reproject(f, Q)[0, 0]).all()
     assert math.isclose(float(opc.reproject(f, Q)[0, 1, 2]), 812.5 / 0.25, rel_tol=1e-7)
+
+
+def test_cli_rejects_missing_qmatrix_before_any_gpu_work(tmp_path):
+    import io
+    with pytest.raises(ValueError, match="does not exist"):
+        cli.main([str(tmp_path), "-q", str(tmp_path / "missing.yml")], out=io.StringIO(), err=io.StringIO())
+
+
+def test_image_round_trips_random_shapes(tmp_path):
+    rng = np.random.default_rng(11)
+    for k in range(25):
+        h, w = int(rng.integers(1, 40)), int(rng.integers(1, 70))
+        dtype = [np.uint8, np.uint16, np.int16, np.float32, np.float64][k % 5]
+        if np.issubdtype(dtype, np.floating):
+            img = rng.normal(scale=100.0, size=(h, w)).astype(dtype)
+        else:
+            info = np.iinfo(dtype)
+            img = rng.integers(info.min, info.max + 1, size=(h, w)).astype(dtype)
+        p = str(tmp_path / f"r{k}.tiff")
+        imageio.write_tiff(p, img)
+        assert np.array_equal(imageio.read_image(p), img), (k, h, w, dtype)
+        if dtype in (np.uint8, np.uint16):
+            q = str(tmp_path / f"r{k}.png")
+            imageio.write_png(q, img)
+            assert np.array_equal(imageio.read_image(q), img), (k, h, w, dtype)
