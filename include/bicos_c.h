@@ -254,7 +254,9 @@ int32_t bicos_png_unfilter(uint8_t* out, const uint8_t* raw, int32_t height, siz
  * host buffers must stay valid until the copy has run.  Pushing a frame
  * again replaces it.  The match runs bicos_match_v1 on the resident frames
  * once every frame has been pushed (BICOS_ERR_EXCEPTION otherwise), ordered
- * after all pushes, on `stream`; outputs as bicos_match_v1.
+ * after all pushes, on `stream`; outputs as bicos_match_v1.  A handle is
+ * used by one host thread at a time; the frames stay resident, so a stack
+ * can be matched again (another configuration) without new pushes.
  */
 typedef struct bicos_ingest bicos_ingest;
 bicos_status bicos_ingest_create(bicos_ingest** out, int32_t rows, int32_t cols, uint32_t n, int32_t type);
