@@ -6,6 +6,9 @@ the oracle independently of the reference build:
   once the sum two steps back exists (the ring starts at -1 = absent), then
   the tail a<b, a<mean, b<mean and "sum two steps back < a+b" (always set
   when that sum is absent, -1 being below any sum);
+* full descriptors for n = 2..5 (descriptor_transform.hpp:75-123): the same
+  per-step and tail bits, then sum[t] < sum[i] for every ordered pair of
+  adjacent-pair sums at least two apart;
 * the search (include/impl/cpu/bicos.hpp:50-113): the first minimum wins;
   with no-duplicates a later equal cost invalidates, but only one seen after
   the last new minimum; the consistency average (col0 + rev) / 2 - best
@@ -71,3 +74,33 @@ def test_search_kat(oracle, costs, flags, lr, want):
     assert got.dtype == np.int16 and got.tolist() == [want]
     if oracle.ref_available():
         assert oracle.search(d0, d1, flags, lr, use_ref=True).tolist() == [want]
+
+
+def _full_cases():
+    # FULL mode (include/impl/cpu/descriptor_transform.hpp:75-123): the same
+    # three bits per step t < n-2 and the tail a<b, a<mean, b<mean, then, for
+    # every ordered pair (t, i) of the n-1 adjacent-pair sums with |t-i| >= 2,
+    # t outer and i inner, the bit sum[t] < sum[i]; n^2 - 2n + 3 bits in all.
+    return [
+        ([10, 20], 0b011),       # tail only: 10<20, 10<15
+        ([20, 10], 0b100),       # 10<15
+        ([7, 7], 0),
+        ([1, 5, 3], 0b000111),   # no pair of sums two apart exists for n=3
+        ([4, 2, 6, 0], 298),     # bits 1, 3, 5, 8; sums 6, 8, 6: 6<6 twice false
+        ([1, 2, 3, 4], 639),     # bits 0..6 and 9 (sum 3 < sum 7); 7 < 3 false
+        ([1, 2, 3, 4, 5], 29439),     # bits 0..7, 9, 12, 13, 14
+        ([5, 4, 3, 2, 1], 232448),    # bits 10, 11 (tail), 15, 16, 17
+    ]
+
+
+@pytest.mark.parametrize("pix,want", _full_cases())
+def test_full_descriptor_kat(oracle, pix, want):
+    n = len(pix)
+    stack = np.array(pix, dtype=np.uint8).reshape(n, 1, 1)
+    d = oracle.transform(stack, True)
+    assert int(d[0, 0, 0]) == want, (pix, bin(int(d[0, 0, 0])), bin(want))
+    assert want < (1 << (n * n - 2 * n + 3))  # nothing past the descriptor's bit count
+    s16 = (stack.astype(np.uint16) * 16).astype(np.uint16)
+    assert int(oracle.transform(s16, True)[0, 0, 0]) == want
+    if oracle.ref_available():
+        assert int(oracle.transform(stack, True, use_ref=True)[0, 0, 0]) == want
