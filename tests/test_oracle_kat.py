@@ -12,7 +12,10 @@ the oracle independently of the reference build:
 * the search (include/impl/cpu/bicos.hpp:50-113): the first minimum wins;
   with no-duplicates a later equal cost invalidates, but only one seen after
   the last new minimum; the consistency average (col0 + rev) / 2 - best
-  truncates, and |col0 - rev| > max_lr_diff invalidates.
+  truncates, and |col0 - rev| > max_lr_diff invalidates;
+* the agreement (include/impl/cpu/agree.hpp:27-185): exact NCC values, the
+  strict variance mask, NaN passing the threshold, out-of-range and border
+  columns, and the sweep's first strictly-better offset on an exact grid.
 """
 import numpy as np
 import pytest
@@ -104,3 +107,103 @@ def test_full_descriptor_kat(oracle, pix, want):
     assert int(oracle.transform(s16, True)[0, 0, 0]) == want
     if oracle.ref_available():
         assert int(oracle.transform(stack, True, use_ref=True)[0, 0, 0]) == want
+
+
+NAN = float("nan")
+
+
+@pytest.mark.parametrize("x,y,min_var,want", [
+    ([0, 2, 4], [1, 3, 5], None, 1.0),    # diffs equal: cov = var0 = var1 = 8
+    ([0, 2, 4], [5, 3, 1], None, -1.0),
+    ([0, 2, 4], [3, 1, 5], None, 0.5),    # cov 4, var 8 and 8
+    ([0, 2, 4], [7, 7, 7], None, NAN),    # 0 / sqrt(0)
+    ([0, 2, 4], [7, 7, 7], 1.0, -1.0),    # variance below the mask
+    ([0, 2, 4], [1, 3, 5], 8.0, 1.0),     # the mask is strict: var 8 is not below 8
+    ([0, 2, 4], [1, 3, 5], 8.5, -1.0),
+])
+def test_nxcorr_kat(oracle, x, y, min_var, want):
+    """include/impl/cpu/agree.hpp:27-50: means, fused sums in frame order,
+    then -1 under the (already n-scaled) variance mask."""
+    for f in (oracle.nxcorr_f, oracle.nxcorr_d):
+        got = f(np.array(x, float), np.array(y, float), min_var)
+        assert (np.isnan(got) and np.isnan(want)) or got == want, (f.__name__, got, want)
+
+
+def _agree_scene():
+    """One row, five columns, n = 3; every left column holds (0, 2, 4)."""
+    s0 = np.array([[0, 2, 4]] * 5, np.uint8).T.reshape(3, 1, 5)
+    right = [[1, 3, 5], [5, 3, 1], [3, 1, 5], [7, 7, 7], [1, 3, 5]]
+    s1 = np.array(right, np.uint8).T.reshape(3, 1, 5)
+    return s0, s1
+
+
+@pytest.mark.parametrize("min_var,want_d,want_c", [
+    # col 0: d=-2 -> right col 2, rho 0.5, not below 0.5: kept
+    # col 1: d=0 -> rho -1: invalid;  col 2: already invalid, no corrmap write
+    # col 3: d=0 -> flat right column: rho NaN, which passes the threshold
+    # col 4: d=5 -> right col -1: invalid, no corrmap write
+    (None, [-2, INV, INV, 0, INV], [0.5, -1.0, NAN, NAN, NAN]),
+    (1.0, [-2, INV, INV, INV, INV], [0.5, -1.0, NAN, -1.0, NAN]),
+])
+def test_agree_kat(oracle, min_var, want_d, want_c):
+    """include/impl/cpu/agree.hpp:52-92."""
+    s0, s1 = _agree_scene()
+    disp = np.array([[-2, 0, INV, 0, 5]], np.int16)
+    for double in (False, True):
+        d, corr = oracle.agree(disp, s0, s1, 0.5, min_var, double=double)
+        assert d.tolist() == [want_d]
+        assert np.array_equal(corr[0], np.array(want_c), equal_nan=True), corr
+    if oracle.ref_available():
+        d, corr = oracle.agree(disp, s0, s1, 0.5, min_var, use_ref=True)
+        assert d.tolist() == [want_d]
+        assert np.array_equal(corr[0], np.array(want_c), equal_nan=True)
+
+
+def _subpixel_scene():
+    """Three rows, five columns, n = 3.  Right columns 1..3 of rows 0-1 are a
+    linear ramp in x per frame (y0 + y2 = 2 y1, so the quadratic term is 0)
+    and the interpolant round(b x + c) is exact on the 0.5 grid."""
+    y0, y1, y2 = [0, 30, 10], [10, 20, 10], [20, 10, 10]
+    s0 = np.zeros((3, 3, 5), np.uint8)
+    s1 = np.zeros((3, 3, 5), np.uint8)
+    # row 0: the left column equals the interpolant at x = +0.5 -> d - 0.5
+    s1[:, 0, 1], s1[:, 0, 2], s1[:, 0, 3] = y0, y1, y2
+    s0[:, 0, 3] = [15, 15, 10]
+    # row 0 borders: right col 0 (rho 1) and right col 4 (rho -1), plain NCC
+    s0[:, 0, 0], s1[:, 0, 0] = [0, 2, 4], [1, 3, 5]
+    s0[:, 0, 4], s1[:, 0, 4] = [0, 2, 4], [5, 3, 1]
+    # row 1: no gradient, every x ties at rho 1: the first, x = -1, is kept
+    s1[:, 1, 1] = s1[:, 1, 2] = s1[:, 1, 3] = y1
+    s0[:, 1, 3] = y1
+    # row 2: a flat left column: under the mask every x gives -1 and none is
+    # strictly better than the initial -1, so x stays 0
+    s1[:, 2, 1], s1[:, 2, 2], s1[:, 2, 3] = y0, y1, y2
+    s0[:, 2, 3] = [7, 7, 7]
+    return s0, s1
+
+
+@pytest.mark.parametrize("thr,min_var,want_d,want_c", [
+    (0.5, 1.0,
+     [[0.0, NAN, NAN, 0.5, NAN], [NAN, NAN, NAN, 2.0, NAN], [NAN, NAN, NAN, NAN, NAN]],
+     [[1.0, NAN, NAN, 1.0, -1.0], [NAN, NAN, NAN, 1.0, NAN], [NAN, NAN, NAN, -1.0, NAN]]),
+    (-1.0, 1.0,  # -1 is not below -1: the border and the masked pixel are kept
+     [[0.0, NAN, NAN, 0.5, 0.0], [NAN, NAN, NAN, 2.0, NAN], [NAN, NAN, NAN, 1.0, NAN]],
+     [[1.0, NAN, NAN, 1.0, -1.0], [NAN, NAN, NAN, 1.0, NAN], [NAN, NAN, NAN, -1.0, NAN]]),
+])
+def test_agree_subpixel_kat(oracle, thr, min_var, want_d, want_c):
+    """include/impl/cpu/agree.hpp:94-185 with step 0.5 (x = -1, -0.5, 0, 0.5, 1)."""
+    s0, s1 = _subpixel_scene()
+    disp = np.full((3, 5), INV, np.int16)
+    disp[0, 0] = 0   # right col 0: border
+    disp[0, 3] = 1   # right col 2
+    disp[0, 4] = 0   # right col 4: border
+    disp[0, 2] = 5   # right col -3: out of range
+    disp[1, 3] = 1
+    disp[2, 3] = 1
+    runs = [dict(double=False), dict(double=True)]
+    if oracle.ref_available():
+        runs.append(dict(use_ref=True))
+    for kw in runs:
+        out, corr = oracle.agree_subpixel(disp, s0, s1, thr, 0.5, min_var, **kw)
+        assert np.array_equal(out, np.array(want_d, np.float32), equal_nan=True), (kw, out)
+        assert np.array_equal(corr, np.array(want_c), equal_nan=True), (kw, corr)
