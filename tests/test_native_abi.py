@@ -149,3 +149,56 @@ def test_ingest_handle_validation(native):
     assert lib.bicos_ingest_destroy(None) == 0
     assert lib.bicos_ingest_push_v1(None, 0, None, None, 8, None) == native.ERR_INVALID_ARGUMENT
     assert lib.bicos_ingest_match_v1(None, None, None, None, None) == native.ERR_INVALID_ARGUMENT
+
+
+C_PROGRAM = r"""
+#include <bicos_c.h>
+#include <stdio.h>
+#include <string.h>
+
+int main(void) {
+    bicos_config c;
+    bicos_image frames[66], disp;
+    int i;
+    if (bicos_config_default(&c) != BICOS_OK || !c.has_threshold || c.nxcorr_threshold != 0.5f ||
+        c.has_subpixel_step || c.mode != BICOS_MODE_LIMITED || c.max_lr_diff != 1)
+        return 10;
+    for (i = 0; i < 66; ++i) { /* never dereferenced: validation fails first */
+        frames[i].data = (void*)0x10; frames[i].step = 16; frames[i].rows = 4; frames[i].cols = 8;
+        frames[i].type = BICOS_8U; frames[i].reserved = 0;
+    }
+    disp = frames[0];
+    disp.type = BICOS_16S;
+    if (bicos_match_v1(frames, frames, 1, &disp, NULL, &c, NULL) != BICOS_ERR_EXCEPTION ||
+        strcmp(bicos_last_error(), "need at least two images") != 0)
+        return 11;
+    if (bicos_match_v1(frames, frames, 66, &disp, NULL, &c, NULL) != BICOS_ERR_INVALID_ARGUMENT ||
+        strcmp(bicos_last_error(), "input stacks too large, would require 257 bits") != 0)
+        return 12;
+    printf("%s\n", bicos_version());
+    return 0;
+}
+"""
+
+
+def test_c_header_is_plain_c(native, tmp_path):
+    """include/bicos_c.h compiles as strict C99 and a C caller links, reads the
+    defaults and gets the reference's error texts (no device work)."""
+    src, exe = tmp_path / "caller.c", tmp_path / "caller"
+    src.write_text(C_PROGRAM)
+    libdir = os.path.dirname(native.lib_path())
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I",
+                    os.path.join(ROOT, "include"), str(src), "-L", libdir, "-lbicos_gb300",
+                    "-Wl,-rpath," + libdir, "-o", str(exe)], check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, (r.returncode, r.stderr)
+    assert "sm_103a" in r.stdout
+
+
+def test_cpp_api_compiles_and_links(native, tmp_path):
+    """The C++ drop-in (include/BICOS/match.hpp) builds against the library
+    the way a libBICOS user's program does; running it needs a GPU."""
+    libdir = os.path.dirname(native.lib_path())
+    subprocess.run(["g++", "-std=c++17", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "match_cpp.cpp"), "-L", libdir, "-lbicos_gb300",
+                    "-Wl,-rpath," + libdir, "-o", str(tmp_path / "match_cpp")], check=True)
