@@ -108,7 +108,7 @@ def cpu_baseline(scene, target_s):
     rows = cpu_sample_rows(scene, cfg, target_s, use_ref)
     mpx, dt = oracle_mpx(scene, rows, cfg, use_ref)
     whole = " (the whole frame: the sample is capped at one full match)" if rows == scene.left.shape[1] else ""
-    return {"value": round(mpx, 4), "unit": METRIC, "cores": O.lib().orc_num_threads(0) if not use_ref else os.cpu_count(),
+    return {"value": round(mpx, 4), "unit": "Mpx/s", "cores": O.lib().orc_num_threads(0) if not use_ref else os.cpu_count(),
             "kind": "reference" if use_ref else "port",
             "sample": f"rows 0..{rows - 1} of the {WORKLOAD} stack (all 1936 columns, n=33){whole}, {dt:.1f} s"}
 
