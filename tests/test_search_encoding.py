@@ -5,7 +5,8 @@ The kernel turns each descriptor bit into an FP8 (e4m3) value whose sign is
 the bit, multiplies query and candidate tiles on the tensor cores and reads
 the arg-min out of the accumulator.  This file restates that integer
 arithmetic (the multiply-and-mask nibble expansion, the e4m3 column code,
-the column-coded keys and their decode) with the byte patterns taken from
+the column-coded keys and their decode, the plain form's FP32 keys
+dot -/+ column/4096 up to the 4096-column bound) with the byte patterns taken from
 the kernel source, decodes every byte with torch's own float8_e4m3fn, and
 checks the decoded result against the oracle's search
 (include/impl/cpu/bicos.hpp:50-113: first minimum, no-duplicates).  The GPU
@@ -154,3 +155,59 @@ def test_coded_keys_match_oracle(oracle, nw, cols):
         results.append(want)
     if cols >= 100:  # both outcomes of the no-duplicates rule occur
         assert 0 < int((results[1] == INV).sum()) < cols
+
+
+def _plain_keys(d0, d1, nodup):
+    """The plain form (descriptor width unknown, every K slot a bit): FP32
+    keys dot - j/4096 and dot + j/4096 in the kernel's operation order
+    (per 32-column chunk: dot -/+ k*s, then -/+ j0*s), decoded by the
+    fractional part."""
+    cols, nw = d0.shape
+    clear = CONST["kClearPlain"]
+    q = np.array([[E4M3[b] for b in expand([int(w) for w in d], clear)] for d in d0])
+    c = np.array([[E4M3[b] for b in expand([int(w) for w in d], clear)] for d in d1])
+    dot = (q @ c.T).astype(np.float32)  # K - 2 * Hamming, exact
+    s = np.float32(1.0 / 4096.0)
+    j = np.arange(cols)
+    k = (j % 32).astype(np.float32)
+    j0 = (j - j % 32).astype(np.float32)
+    ka = (dot - k * s) - j0 * s
+    kb = (dot + k * s) + j0 * s
+    assert ka.dtype == np.float32
+    ma, mb = ka.max(axis=1), kb.max(axis=1)
+    best = ((np.ceil(ma) - ma) * np.float32(4096.0)).astype(np.int64)
+    last = ((mb - np.floor(mb)) * np.float32(4096.0)).astype(np.int64)
+    valid = (last == best) if nodup else np.ones(cols, bool)
+    return np.where(valid, j - best, INV)
+
+
+@pytest.mark.parametrize("nw", [1, 2, 4, 8])
+@pytest.mark.parametrize("cols", [1, 33, 300])
+def test_plain_keys_match_oracle(oracle, nw, cols):
+    rng = np.random.default_rng(nw * 77 + cols)
+    d1 = rng.integers(0, 2 ** 32, size=(cols, nw), dtype=np.uint64).astype(np.uint32)
+    dup = rng.random(cols) < 1 / 3
+    d1[dup] = d1[rng.integers(0, cols, size=int(dup.sum()))]
+    d0 = d1[rng.integers(0, cols, size=cols)].copy()
+    flips = np.bitwise_and.reduce(rng.integers(0, 2 ** 32, size=(4, cols, nw), dtype=np.uint64).astype(np.uint32))
+    d0 ^= flips
+    for nodup in (False, True):
+        want = oracle.search(d0.reshape(1, cols, nw), d1.reshape(1, cols, nw), int(nodup))[0]
+        assert np.array_equal(_plain_keys(d0, d1, nodup), want.astype(np.int64)), (nw, cols, nodup)
+
+
+def test_widest_row_both_forms(oracle):
+    """4096 columns, the width bound of the tensor-core search: the last
+    column's keys stay exact in both forms."""
+    cols, nw = 4096, 1
+    rng = np.random.default_rng(5)
+    d1 = (rng.integers(0, 2 ** 30, size=(cols, nw), dtype=np.uint64)).astype(np.uint32)
+    d1[-1] = d1[0]          # the minimum of query 0 at the first and the last column
+    d1[-2] = d1[-3]
+    d0 = d1[[0, cols - 1, cols - 2, cols - 3] + list(rng.integers(0, cols, size=cols - 4))].copy()
+    for nodup in (False, True):
+        want = oracle.search(d0.reshape(1, cols, nw), d1.reshape(1, cols, nw), int(nodup))[0].astype(np.int64)
+        assert np.array_equal(_plain_keys(d0, d1, nodup), want), nodup
+        sub = slice(0, 64)  # the coded model is slower: a prefix of the queries, all candidates
+        assert np.array_equal(_keys(d0, d1, nodup)[sub], want[sub]), nodup
+    assert want[0] == INV and want[1] == INV  # duplicated minima under no-duplicates
