@@ -114,6 +114,14 @@ def search(desc0, desc1, flags: int, max_lr_diff: int = -1, stream=None, bits=No
     disparity.  bits: the descriptors' bit count when known (higher bits
     zero, as the transform writes them; bicos_search_bits_v1)."""
     import torch
+    # the C call takes bare pointers and the sizes of desc0: both tensors
+    # must hold exactly rows x cols x nwords 32-bit words on the device
+    if desc0.dim() != 3 or tuple(desc1.shape) != tuple(desc0.shape):
+        raise ValueError(f"descriptors must be (rows, cols, nwords) tensors of one shape, got "
+                         f"{tuple(desc0.shape)} and {tuple(desc1.shape)}")
+    for d in (desc0, desc1):
+        if not d.is_cuda or not d.is_contiguous() or d.element_size() != 4 or d.dtype.is_floating_point:
+            raise ValueError("descriptors must be contiguous 32-bit integer CUDA tensors")
     rows, cols, nw = desc0.shape
     out = torch.empty((rows, cols), dtype=torch.int16, device=desc0.device)
     oi = N.tensor_image(out)
@@ -234,16 +242,28 @@ class Ingest:
         except Exception:
             pass
 
-    @staticmethod
-    def _host(a):
-        if hasattr(a, "data_ptr"):  # torch CPU tensor
-            if a.dim() != 2 or a.stride(1) != 1:
-                raise ValueError("expected 2-D frames with unit column stride")
+    def _host(self, a):
+        """(keep-alive object, host pointer, row step) of one frame, checked
+        against the handle's shape and sample type: the C call copies
+        rows x cols samples from the pointer and cannot check the buffer."""
+        esize = 1 if self._type == N.BICOS_8U else 2
+        if hasattr(a, "data_ptr"):  # torch tensor
+            if a.device.type != "cpu":
+                raise ValueError("frames are host buffers: numpy arrays or CPU torch tensors")
+            if a.dtype.is_floating_point or a.dtype.is_complex or str(a.dtype) == "torch.bool" \
+                    or a.element_size() != esize:
+                raise ValueError(f"expected {8 * esize}-bit integer frames, got {a.dtype}")
+            if tuple(a.shape) != (self.rows, self.cols) or a.stride(1) != 1:
+                raise ValueError(f"expected {self.rows}x{self.cols} frames with unit column stride, "
+                                 f"got shape {tuple(a.shape)}")
             return a, a.data_ptr(), a.stride(0) * a.element_size()
         import numpy as np
         a = np.ascontiguousarray(a)
-        if a.ndim != 2:
-            raise ValueError("expected 2-D frames")
+        want = np.uint8 if esize == 1 else np.uint16
+        if a.dtype != want:
+            raise ValueError(f"expected {np.dtype(want).name} frames, got {a.dtype}")
+        if a.shape != (self.rows, self.cols):
+            raise ValueError(f"expected {self.rows}x{self.cols} frames, got shape {a.shape}")
         return a, a.ctypes.data, a.strides[0]
 
     def push(self, t: int, left, right, stream=None):

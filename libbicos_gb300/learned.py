@@ -182,9 +182,25 @@ def _ptr(t):
     return C.c_void_p(t.data_ptr())
 
 
+def _check(t, name, min_numel=None, row=None):
+    """The MLP entry points take bare device pointers and a row count:
+    each buffer must be a contiguous float32 CUDA tensor of the size the
+    kernel reads or writes."""
+    if not t.is_cuda or not t.is_contiguous() or str(t.dtype) != "torch.float32":
+        raise ValueError(f"{name}: expected a contiguous float32 CUDA tensor")
+    if row is not None and (t.dim() != 2 or t.shape[1] != row):
+        raise ValueError(f"{name}: expected (count, {row}) rows, got shape {tuple(t.shape)}")
+    if min_numel is not None and t.numel() < min_numel:
+        raise ValueError(f"{name}: expected at least {min_numel} floats, got {t.numel()}")
+
+
 def grad(model, samples, grad_buf, loss_buf, stream=None):
     """Adds the batch's gradient to grad_buf and its loss to loss_buf."""
     import torch
+    _check(model, "model", MODEL_FLOATS)
+    _check(samples, "samples", row=N_IN + 1)
+    _check(grad_buf, "grad_buf", N_PARAMS)
+    _check(loss_buf, "loss_buf", 1)
     st = C.c_void_p((stream or torch.cuda.current_stream()).cuda_stream)
     N.check(N.load().bicos_mlp_grad_v1(_ptr(model), _ptr(samples), samples.shape[0], _ptr(grad_buf),
                                        _ptr(loss_buf), st))
@@ -192,6 +208,8 @@ def grad(model, samples, grad_buf, loss_buf, stream=None):
 
 def adam(model, grad_buf, m, v, step, lr, scale, stream=None):
     import torch
+    for t, name in ((model, "model"), (grad_buf, "grad_buf"), (m, "m"), (v, "v")):
+        _check(t, name, N_PARAMS)
     st = C.c_void_p((stream or torch.cuda.current_stream()).cuda_stream)
     N.check(N.load().bicos_mlp_adam_v1(_ptr(model), _ptr(grad_buf), _ptr(m), _ptr(v), step, lr, scale, st))
 
@@ -199,6 +217,8 @@ def adam(model, grad_buf, m, v, step, lr, scale, stream=None):
 def propose(model, feats, stream=None):
     """Proposals of the inference kernel for (N, 8) feature rows."""
     import torch
+    _check(model, "model", MODEL_FLOATS)
+    _check(feats, "feats", row=N_IN + 1)
     out = torch.empty(feats.shape[0], dtype=torch.float32, device=feats.device)
     st = C.c_void_p((stream or torch.cuda.current_stream()).cuda_stream)
     N.check(N.load().bicos_mlp_propose_v1(_ptr(model), _ptr(feats), feats.shape[0], _ptr(out), st))

@@ -202,3 +202,92 @@ def test_cpp_api_compiles_and_links(native, tmp_path):
     subprocess.run(["g++", "-std=c++17", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
                     os.path.join(ROOT, "tests", "cpp", "match_cpp.cpp"), "-L", libdir, "-lbicos_gb300",
                     "-Wl,-rpath," + libdir, "-o", str(tmp_path / "match_cpp")], check=True)
+
+
+def test_ingest_frame_checks_on_host():
+    """Ingest.push checks each frame against the handle before the C call,
+    which copies rows x cols samples from a bare pointer."""
+    import torch
+    import libbicos_gb300 as lbg
+    from libbicos_gb300 import _native as N
+    ing = lbg.Ingest.__new__(lbg.Ingest)  # no device handle: only the host checks run
+    ing.rows, ing.cols, ing.n, ing._type, ing._h, ing._keep = 4, 8, 3, N.BICOS_8U, None, {}
+    ok = np.zeros((4, 8), np.uint8)
+    assert ing._host(ok)[2] == 8
+    assert ing._host(torch.zeros((4, 8), dtype=torch.uint8))[2] == 8
+    assert ing._host(np.zeros((4, 16), np.uint8)[:, ::2])[2] == 8  # made contiguous
+    bad = [np.zeros((4, 7), np.uint8), np.zeros((3, 8), np.uint8), np.zeros((4, 8), np.uint16),
+           np.zeros((4, 8), np.float32), np.zeros((2, 4, 8), np.uint8),
+           torch.zeros((4, 8), dtype=torch.float32), torch.zeros((4, 8), dtype=torch.bool),
+           torch.zeros((4, 8), dtype=torch.uint8, device="meta"), torch.zeros((8, 4), dtype=torch.uint8).t()]
+    for b in bad:
+        with pytest.raises(ValueError):
+            ing.push(0, b, ok)
+        with pytest.raises(ValueError):
+            ing.push(0, ok, b)
+    ing._type = N.BICOS_16U
+    assert ing._host(np.zeros((4, 8), np.uint16))[2] == 16
+    with pytest.raises(ValueError):
+        ing._host(ok)
+
+
+class _FakeDevice:
+    """Stands in for a CUDA tensor in host-side argument checks (no GPU
+    here): shape and dtype of a CPU tensor, reported as on the device."""
+    is_cuda = True
+
+    def __init__(self, *shape, dtype=None):
+        import torch
+        self._t = torch.zeros(*shape, dtype=dtype or torch.float32)
+        self.shape, self.dtype = self._t.shape, self._t.dtype
+
+    def is_contiguous(self):
+        return True
+
+    def dim(self):
+        return self._t.dim()
+
+    def numel(self):
+        return self._t.numel()
+
+    def element_size(self):
+        return self._t.element_size()
+
+
+def test_mlp_buffer_checks_on_host():
+    """The MLP entry points take bare pointers: the wrappers check every
+    buffer's residency, type and size before the call."""
+    import torch
+    from libbicos_gb300 import learned as L
+    F = _FakeDevice
+    model, params = F(L.MODEL_FLOATS), F(L.N_PARAMS)
+    rows = F(10, L.N_IN + 1)
+    L._check(model, "model", L.MODEL_FLOATS)
+    L._check(rows, "rows", row=8)
+    bad_calls = [
+        lambda: L.grad(F(L.N_PARAMS), rows, params, F(1)),          # model without input statistics
+        lambda: L.grad(model, F(10, 7), params, F(1)),               # rows of 7
+        lambda: L.grad(model, rows, F(L.N_PARAMS - 1), F(1)),
+        lambda: L.grad(model, rows, params, F(0)),
+        lambda: L.grad(model, F(10, 8, dtype=torch.float64), params, F(1)),
+        lambda: L.grad(torch.zeros(L.MODEL_FLOATS), rows, params, F(1)),  # host tensor
+        lambda: L.adam(params, params, F(L.N_PARAMS - 1), params, 1, 1e-3, 1.0),
+        lambda: L.propose(model, F(10, 9)),
+        lambda: L.propose(F(L.N_PARAMS), rows),
+    ]
+    for call in bad_calls:
+        with pytest.raises(ValueError):
+            call()
+
+
+def test_search_descriptor_checks_on_host():
+    import torch
+    import libbicos_gb300 as lbg
+    F = _FakeDevice
+    a = F(2, 16, 4, dtype=torch.int32)
+    for d0, d1 in [(a, F(2, 15, 4, dtype=torch.int32)), (a, F(2, 16, 2, dtype=torch.int32)),
+                   (a, F(2, 16, 4, dtype=torch.float32)), (a, F(2, 16, 4, dtype=torch.int64)),
+                   (F(32, 4, dtype=torch.int32), F(32, 4, dtype=torch.int32)),
+                   (a, torch.zeros((2, 16, 4), dtype=torch.int32))]:
+        with pytest.raises(ValueError, match="descriptors"):
+            lbg.search(d0, d1, 0)
