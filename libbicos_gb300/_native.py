@@ -144,7 +144,10 @@ def type_of(dtype) -> int:
 
 
 def tensor_image(t) -> Image:
-    """bicos_image view of a 2-D CUDA tensor (row-contiguous, any row pitch)."""
+    """bicos_image view of a 2-D CUDA tensor (row-contiguous, any row pitch).
+    Kernels write through these views, so host memory is refused here."""
+    if not t.is_cuda:
+        raise ValueError("expected a CUDA tensor (device memory)")
     if t.dim() != 2 or t.stride(1) != 1:
         raise ValueError("expected a 2-D tensor with unit column stride")
     return image(t.data_ptr(), t.shape[0], t.shape[1], type_of(t.dtype), t.stride(0) * t.element_size())
@@ -156,6 +159,8 @@ TYPE_32FC3 = 21
 def points_image(t) -> Image:
     """bicos_image view of a (rows, cols, 3) float32 CUDA tensor (packed
     pixels, any row pitch)."""
+    if not t.is_cuda:
+        raise ValueError("expected a CUDA tensor (device memory)")
     if t.dim() != 3 or t.shape[2] != 3 or t.stride(2) != 1 or t.stride(1) != 3 or str(t.dtype) != "torch.float32":
         raise ValueError("expected a (rows, cols, 3) float32 tensor with packed pixels")
     return image(t.data_ptr(), t.shape[0], t.shape[1], TYPE_32FC3, t.stride(0) * 4)

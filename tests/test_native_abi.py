@@ -291,3 +291,18 @@ def test_search_descriptor_checks_on_host():
                    (a, torch.zeros((2, 16, 4), dtype=torch.int32))]:
         with pytest.raises(ValueError, match="descriptors"):
             lbg.search(d0, d1, 0)
+
+
+def test_device_views_refuse_host_memory():
+    """Kernels write through bicos_image views of tensors: a host tensor
+    (an `out` buffer, a disparity to agree on) is refused before any call."""
+    import torch
+    import libbicos_gb300 as lbg
+    from libbicos_gb300 import _native as N
+    h16 = torch.zeros((4, 8), dtype=torch.int16)
+    with pytest.raises(ValueError, match="CUDA"):
+        N.tensor_image(h16)
+    with pytest.raises(ValueError, match="CUDA"):
+        N.points_image(torch.zeros((4, 8, 3), dtype=torch.float32))
+    with pytest.raises(ValueError, match="CUDA"):
+        lbg.reproject(h16, np.eye(4))
