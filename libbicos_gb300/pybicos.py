@@ -155,7 +155,9 @@ def _as_image(a) -> np.ndarray:
         raise Exception(f"expected 2-D images, got shape {a.shape}")
     if a.dtype not in (np.uint8, np.uint16):
         raise Exception(f"unimplemented cvtype_of(dtype={a.dtype})")
-    if a.strides[1] != a.itemsize:
+    # unit column stride and a forward row step of at least one row (a
+    # flipped view's negative step would reach the C call as a huge size_t)
+    if a.strides[1] != a.itemsize or a.strides[0] < a.shape[1] * a.itemsize:
         a = np.ascontiguousarray(a)
     return a
 

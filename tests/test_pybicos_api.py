@@ -58,3 +58,16 @@ def test_too_large_is_value_error(native):
     cfg.mode = pybicos.Full
     with pytest.raises(ValueError, match="would require 258 bits"):
         pybicos.match([z] * 17, [z] * 17, cfg)
+
+
+def test_host_images_get_a_forward_row_step():
+    """Views with negative or overlapping row steps become contiguous copies
+    before their pointers reach the host-buffer call."""
+    import numpy as np
+    from libbicos_gb300.pybicos import _as_image
+    a = np.arange(6 * 8, dtype=np.uint8).reshape(6, 8)
+    for v in (a[::-1], a[:, ::-1], a[::-2], np.lib.stride_tricks.as_strided(a, (6, 8), (0, 1))):
+        img = _as_image(v)
+        assert img.strides[1] == 1 and img.strides[0] >= 8
+        assert np.array_equal(img, v)
+    assert _as_image(a[:, :4]).strides[0] == 8  # a padded row step is kept (no copy)
