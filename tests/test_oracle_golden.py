@@ -77,3 +77,21 @@ def test_double_nxcorr_close_to_float(oracle):
         f, d = oracle.nxcorr_f(x, y), oracle.nxcorr_d(x, y)
         if np.isfinite(d):
             assert abs(f - d) <= 1e-5
+
+
+def test_oracle_independent_of_threads(oracle):
+    """The restatement splits rows over threads (the CPU baseline uses all
+    cores); every stage gives the same bits with 1, 3 or all threads."""
+    from libbicos_gb300 import scenes
+    sc = scenes.make_scene(37, 90, 12, seed=21)
+    runs = []
+    for nt in (1, 3, 0):
+        cfg = oracle.make_config(threshold=0.9, step=0.1, min_variance=2.0)
+        d, c = oracle.match(sc.left, sc.right, cfg, nthreads=nt)
+        desc = oracle.transform(sc.left, False, nthreads=nt)
+        cons = oracle.match(sc.left, sc.right, oracle.make_config(threshold=0.5, consistency=(1, True)),
+                            nthreads=nt)[0]
+        runs.append((d, c, desc, cons))
+    for r in runs[1:]:
+        for a, b in zip(runs[0], r):
+            assert np.array_equal(a, b, equal_nan=True)
