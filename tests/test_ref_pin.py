@@ -68,3 +68,24 @@ def test_errors_match_reference(ref):
     for use_ref in (False, True):
         with pytest.raises(ref.OracleError, match="would require 258 bits"):
             ref.match(s, s, cfg, use_ref=use_ref)
+
+
+def test_golden_files_regenerate(ref):
+    """tests/golden/*.npz are what tests/golden/make_golden.py computes from
+    the reference build: regenerated here in memory, every array equal."""
+    import importlib.util
+    import os
+    from conftest import ROOT
+    path = os.path.join(ROOT, "tests", "golden", "make_golden.py")
+    spec = importlib.util.spec_from_file_location("make_golden", path)
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    rng = np.random.default_rng(20241203)  # the generator's seed, in its call order
+    fresh = {"transform": mg.transform_cases(rng), "search": mg.search_cases(rng),
+             "agree": mg.agree_cases(rng), "match": mg.match_cases()}
+    for name, arrays in fresh.items():
+        with np.load(os.path.join(ROOT, "tests", "golden", name + ".npz")) as z:
+            assert sorted(z.files) == sorted(arrays), name
+            for k, v in arrays.items():
+                want = np.asarray(v)
+                assert np.array_equal(z[k], want, equal_nan=want.dtype.kind in "fc"), (name, k)
