@@ -13,8 +13,10 @@
 // every product is an integer below 2^16 and every sum below 2^24, so the
 // FP32 results are exact for 8-bit stacks (n <= 65).  12-bit data is split
 // into 6-bit halves, x = 64 xh + xl: Sxy = 4096 (xh.yh) + 64 (xh.yl +
-// xl.yh) + xl.yl from three accumulators.  Tiles whose disparities spread
-// wider than the window use SIMT dot products (the same integers).
+// xl.yh) + xl.yl from three accumulators, exact for samples below 4096;
+// wider 16-bit samples give xh up to 1023, and the xh.yh sums can pass 2^24
+// and round.  Tiles whose disparities spread wider than the window use SIMT
+// dot products (the same integers).
 //
 // Leaving the sweep's quadratic interpolant unrounded, I(x) = a x^2 + b x + c
 // (a, b, c from y at col1-1, col1, col1+1), the sweep correlation is

@@ -94,3 +94,26 @@ def test_small_int_to_float_exhaustive():
     u = (np.int64(0x4B400000) + v).astype(np.uint32)
     got = (u.view(F32) - MAGIC).astype(F32)
     assert np.array_equal(got, v.astype(F32))
+
+
+def test_moment_band_exactness_bounds():
+    """The moment form's tensor-core band (csrc/moments.cu): FP16 operands,
+    FP32 sums.  Every operand must be an FP16 integer (below 2048) and every
+    partial sum below 2^24 for the band to be exact."""
+    n_max = 65
+    assert 255 * 255 * n_max < 2 ** 24                      # 8-bit samples
+    hi, lo = 4095 >> 6, 4095 & 63                           # 12-bit: 6 + 6 bits
+    assert max(hi, lo) < 2048
+    assert hi * hi * n_max < 2 ** 24                        # xh . yh
+    assert (hi * lo + lo * hi) * n_max < 2 ** 24            # xh . yl + xl . yh (one accumulator)
+    assert lo * lo * n_max < 2 ** 24
+    x = np.arange(4096, dtype=np.int64)
+    assert np.array_equal(4096 * ((x >> 6) * (x >> 6)) + 64 * (2 * (x >> 6) * (x & 63)) + (x & 63) ** 2, x * x)
+    # past 12 bits the high part reaches 1023 and its sums pass 2^24 from
+    # n = 17 on: the documented limit of the form
+    hi16 = 65535 >> 6
+    assert hi16 < 2048 and hi16 * hi16 * 16 < 2 ** 24 <= hi16 * hi16 * 17
+    s = np.float32(0)
+    for _ in range(17):
+        s = np.float32(s + np.float32(hi16 * hi16))
+    assert int(s) != 17 * hi16 * hi16                       # FP32 accumulation rounds there
