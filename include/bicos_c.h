@@ -292,7 +292,8 @@ bicos_status bicos_agree_subpixel_v1(const bicos_image* raw_disparity, const bic
  *   into `features` (float32, rows x 8*cols, 16-byte aligned rows): the
  *   correlation of the left pixel with the right columns col1-2..col1+2
  *   (NaN outside the image), the left and right per-frame variances, and 1
- *   (0 and NaNs for invalid matches).  Exact integer moments, FP32 ratio.
+ *   (0 and NaNs for invalid matches).  Exact integer moments (for 8-bit
+ *   and 12-bit data, as the MOMENTS form), FP32 ratio.
  * bicos_agree_learned_v1: the LEARNED agreement stage of a raw disparity,
  *   arguments as bicos_agree_subpixel_v1 (min_var already scaled by n);
  *   optionally the network's proposals (float32 image) and, after the
