@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--no-double", action="store_true")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned subpixel form")
     ap.add_argument("--no-batch", action="store_true", help="skip the 16-stack batch comparison")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the 640x480 and the 2048x1536 12-bit precision-form workloads")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target CPU work of the baseline sample")
     return ap.parse_args()
 
@@ -101,6 +103,16 @@ def cpu_sample_rows(scene, cfg, target_s, use_ref=False):
     return int(max(probe, min(scene.left.shape[1], target_s / max(dt / probe, 1e-6))))
 
 
+# The C restatement (oracle/bicos_oracle.c, "port") against libBICOS's own
+# CPU backend built from its sources (oracle/ref_build.sh), same host, same
+# 48 rows of the production stack, all threads: measured on an 8-core x86
+# host (the GPU hosts carry no reference sources), port 0.38-0.40 Mpx/s,
+# reference build 0.29-0.36 Mpx/s.  Where only the port runs, the CPU
+# numbers here are, if anything, faster than the reference's own.
+PORT_VS_REFERENCE = ("the port ran at about 1.2x the reference build's speed on the same 8-core x86 host "
+                     "(0.38 vs 0.31 Mpx/s on 48 rows of this stack), so it does not flatter the GPU ratio")
+
+
 def cpu_baseline(scene, target_s):
     from oracle import oracle as O
     cfg = O.make_config(threshold=THRESHOLD, step=STEP, min_variance=MIN_VAR)
@@ -113,7 +125,8 @@ def cpu_baseline(scene, target_s):
     return {"value": round(mpx, 4), "unit": "Mpx/s", "cores": O.lib().orc_num_threads(0) if not use_ref else os.cpu_count(),
             "kind": "reference" if use_ref else "port",
             "sample": f"rows 0..{rows - 1} of the {WORKLOAD} stack (all 1936 columns, n=33){whole}, "
-                      f"median of 3 runs, {dt:.1f} s in all"}
+                      f"median of 3 runs, {dt:.1f} s in all"
+                      + ("" if use_ref else f"; {PORT_VS_REFERENCE}")}
 
 
 class ClockSampler:
@@ -194,51 +207,64 @@ def profile_traffic(kernel):
     return None
 
 
-def stage_rooflines(stages, rows, cols, n, clk, valid=0.806):
+def stage_rooflines(stages, rows, cols, n, clk, valid=0.806, eb=1, nwords=4, dirs=1, full=False,
+                    agree="subpixel_f32", positions=21):
     """Roofline of each stage from its live CUDA-event time (ms per launch).
 
-    transform: HBM, bytes 2*px*n + 2*px*16 (u8 stack in, 128-bit words out)
-    search:    tensor, 2*rows*cols^2*128 FLOP (+-1 FP8 dot products, one
-               direction) against the FP8 dense rate taken as twice the
-               measured bf16 GEMM rate
-    subpixel:  HBM, bytes 2*px*n (stack in) + px*8 (float disparity and
-               corrmap out); its FP32 view (12 flops per valid pixel, sweep
-               position and frame, 21 positions at step 0.1, against the
-               FP32 vector peak 152 SMs x 128 lanes x 2 x SM clock) rides
-               along under "fp32"
+    transform: HBM, bytes 2*px*n*eb (stack in) + 2*px*4*nwords (words out)
+    search:    tensor, 2*rows*cols^2*32*nwords FLOP per direction (+-1 FP8
+               dot products over the padded descriptor width) against the
+               FP8 dense rate taken as twice the measured bf16 GEMM rate
+    agreement: HBM, bytes 2*px*n*eb (stack in) + px*(2 or 4) disparity
+               out + px*(4 or 8) corrmap out (+ px*2 raw disparity in);
+               the single-precision sweep's FP32 view (12 flops per valid
+               pixel, sweep position and frame, against the FP32 vector
+               peak 152 SMs x 128 lanes x 2 x SM clock) rides along under
+               "fp32"
+    agree: the agreement kernel ("subpixel_f32", "subpixel_f64", "agree",
+    "moments"); positions: sweep positions per pixel (21 at step 0.1).
     """
     hbm, bf16, src = peaks()
     px = rows * cols
     sm_mhz = clk.get("sm_mhz") or 2070.0
     t_tf, t_se, t_ag = [max(x, 1e-9) for x in stages]
-    tf_bytes = 2 * px * n + 2 * px * 16
-    se_flop = 2.0 * rows * cols * cols * 128
-    ag_bytes = 2 * px * n + px * 8
-    ag_flop = 12.0 * valid * px * 21 * n
+    tf_bytes = 2 * px * n * eb + 2 * px * 4 * nwords
+    se_flop = 2.0 * rows * cols * cols * 32 * nwords * dirs
+    dbl = agree in ("subpixel_f64", "moments")
+    sweep = agree.startswith("subpixel") or agree == "moments"
+    ag_bytes = 2 * px * n * eb + px * (4 if sweep else 2) + px * (8 if dbl else 4) + px * 2
     fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
     fp8_peak = 2 * bf16
+    tf_kernel = "k_transform_full" if full else "k_transform_limited"
+    ag_kernel = {"subpixel_f32": "k_subpixel_f32", "subpixel_f64": "k_subpixel_f64", "agree": "k_agree",
+                 "moments": "k_moments"}[agree]
 
     def gbs(b, t):
         return b / (t * 1e-3) / 1e9
-    return {
-        "transform": {"kernel": "k_transform_limited", "bound": "hbm", "ms": round(t_tf, 4),
+    out = {
+        "transform": {"kernel": tf_kernel, "bound": "hbm", "ms": round(t_tf, 4),
                       "achieved": round(gbs(tf_bytes, t_tf), 1), "peak": hbm, "unit": "GB/s",
                       "frac": round(gbs(tf_bytes, t_tf) / hbm, 4), "peak_source": f"{src} HBM copy bandwidth",
-                      "traffic": profile_traffic("k_transform_limited"), "algorithmic_bytes": tf_bytes},
+                      "traffic": profile_traffic(tf_kernel), "algorithmic_bytes": tf_bytes},
         "search": {"kernel": "k_search_tc", "bound": "tensor", "ms": round(t_se, 4),
                    "achieved": round(se_flop / (t_se * 1e-3) / 1e12, 1), "peak": round(fp8_peak, 1),
                    "unit": "TFLOP/s", "frac": round(se_flop / (t_se * 1e-3) / 1e12 / fp8_peak, 4),
                    "peak_source": f"FP8 dense = 2 x {src} bf16 GEMM rate",
-                   "traffic": profile_traffic("k_search_tc"), "algorithmic_flop": se_flop},
-        "subpixel": {"kernel": "k_subpixel_f32", "bound": "hbm", "ms": round(t_ag, 4),
-                     "achieved": round(gbs(ag_bytes, t_ag), 1), "peak": hbm, "unit": "GB/s",
-                     "frac": round(gbs(ag_bytes, t_ag) / hbm, 4), "peak_source": f"{src} HBM copy bandwidth",
-                     "traffic": profile_traffic("k_subpixel_f32"), "algorithmic_bytes": ag_bytes,
-                     "fp32": {"achieved": round(ag_flop / (t_ag * 1e-3) / 1e12, 2), "peak": round(fp32_peak, 1),
-                              "unit": "TFLOP/s", "frac": round(ag_flop / (t_ag * 1e-3) / 1e12 / fp32_peak, 4),
-                              "peak_source": f"FP32 vector peak at the median SM clock {sm_mhz:.0f} MHz",
-                              "algorithmic_flop": ag_flop}},
+                   "traffic": profile_traffic("k_search_tc"), "algorithmic_flop": se_flop,
+                   "directions": dirs},
+        "agreement": {"kernel": ag_kernel, "bound": "hbm", "ms": round(t_ag, 4),
+                      "achieved": round(gbs(ag_bytes, t_ag), 1), "peak": hbm, "unit": "GB/s",
+                      "frac": round(gbs(ag_bytes, t_ag) / hbm, 4), "peak_source": f"{src} HBM copy bandwidth",
+                      "traffic": profile_traffic(ag_kernel), "algorithmic_bytes": ag_bytes},
     }
+    if agree == "subpixel_f32":
+        ag_flop = 12.0 * valid * px * positions * n
+        out["agreement"]["fp32"] = {
+            "achieved": round(ag_flop / (t_ag * 1e-3) / 1e12, 2), "peak": round(fp32_peak, 1),
+            "unit": "TFLOP/s", "frac": round(ag_flop / (t_ag * 1e-3) / 1e12 / fp32_peak, 4),
+            "peak_source": f"FP32 vector peak at the median SM clock {sm_mhz:.0f} MHz",
+            "algorithmic_flop": ag_flop}
+    return out
 
 
 def batch_bench(lbg, pybicos, scenes, seed, rounds=3, specs=None):
@@ -296,6 +322,80 @@ def batch_bench(lbg, pybicos, scenes, seed, rounds=3, specs=None):
             "graph_captures": b.captures,
             "data": "seeded synthetic stacks generated on the GPU (make_scene_device), threshold 0.9, "
                     "min_variance 2.0"}
+
+
+def moment_form_error(d_ref, c_ref, d_mom, c_mom):
+    """|d rho| and |d disparity| of the moment form against the reference
+    form (both double precision) on pixels valid in both, and the share of
+    pixels whose validity agrees."""
+    import torch
+    both = torch.isfinite(d_ref) & torch.isfinite(d_mom)
+    dd = (d_mom[both].double() - d_ref[both].double()).abs()
+    dr = (c_mom[both] - c_ref[both]).abs()
+
+    def q(v, p):
+        return float(torch.quantile(v[torch.randperm(v.numel(), device=v.device)[:1 << 24]], p))
+    return {"pixels_valid_in_both": int(both.sum()),
+            "validity_agreement": round(float((torch.isfinite(d_ref) == torch.isfinite(d_mom)).double().mean()), 6),
+            "rho_abs_err": {"median": q(dr, 0.5), "p95": q(dr, 0.95), "max": float(dr.max())},
+            "disparity_abs_err_px": {"median": q(dd, 0.5), "p95": q(dd, 0.95), "max": float(dd.max()),
+                                     "rms": float(torch.sqrt(torch.mean(dd ** 2)))}}
+
+
+def config_benches(lbg, pybicos, scenes, timed_match, clk, seed, steps):
+    """The two other seeded workloads, each timed like the headline one:
+    c0 -- 640x480 uint8, n=12, limited (64-bit words), threshold 0.9,
+    min_variance 2.0, no subpixel, NoDuplicates, single precision;
+    c2 -- 2048x1536 12-bit (uint16), n=20, FULL descriptors (363 bits, the
+    512-bit extension), Consistency{1}, threshold 0.9, step 0.1: the
+    reference form in double precision and the moment form (Sxy on the
+    tensor cores, exact int64 moments, FP64 cross term), with the moment
+    form's error against the reference form's FP64 results."""
+    import torch
+    dev = torch.device("cuda", torch.cuda.current_device())
+    out = {}
+    sc = scenes.workload_scene("vga_n12", seed=seed)
+    n, rows, cols = sc.left.shape
+    left, right = torch.from_numpy(sc.left).to(dev), torch.from_numpy(sc.right).to(dev)
+    c = pybicos.Config()
+    c.nxcorr_threshold, c.min_variance = 0.9, 2.0
+    ms, st, o = timed_match(left, right, c, steps * 4, 5, stage_times=True)
+    valid = float((o[0] != -32768).float().mean())
+    c0 = {"value": round(rows * cols / (ms * 1e-3) / 1e6, 3), "unit": "Mpx/s", "ms_per_step": round(ms, 4),
+          "config": "640x480 uint8, n=12, limited (41 bits -> 64-bit words), threshold 0.9, min_variance 2.0, "
+                    "no subpixel, NoDuplicates, single precision",
+          "l2": "inputs (7.4 MB) fit in L2: back-to-back calls, warm L2",
+          "valid_fraction": round(valid, 4),
+          "stage_ms": {"transform": round(st[0], 4), "search": round(st[1], 4), "agreement": round(st[2], 4)},
+          "stage_rooflines": stage_rooflines(st, rows, cols, n, clk, valid, nwords=2, agree="agree")}
+    del left, right
+
+    sc = scenes.workload_scene("qxga12_n20", seed=seed)
+    n, rows, cols = sc.left.shape
+    left, right = torch.from_numpy(sc.left).to(dev), torch.from_numpy(sc.right).to(dev)
+    res = {"config": "2048x1536 12-bit samples in uint16, n=20, FULL descriptors (363 bits -> 384-bit words, "
+                     "the max_bits=512 extension: libBICOS throws for this stack), Consistency{max_lr_diff=1}, "
+                     "threshold 0.9, step 0.1, precision double",
+           "l2": "inputs larger than L2: 252 MB of frames per step (L2 129 MB)"}
+    outs = {}
+    for name, form in (("reference_form", 0), ("moment_form", 1)):
+        c = pybicos.Config()
+        c.nxcorr_threshold, c.subpixel_step = 0.9, 0.1
+        c.mode, c.precision, c.nxcorr_form = pybicos.Full, pybicos.Double, form
+        c.variant = pybicos.Variant.Consistency(1, False)
+        ms, st, o = timed_match(left, right, c, steps, 2, stage_times=True, max_bits=512)
+        outs[name] = o
+        valid = float(torch.isfinite(o[0]).float().mean())
+        res[name] = {"value": round(rows * cols / (ms * 1e-3) / 1e6, 3), "unit": "Mpx/s",
+                     "ms_per_step": round(ms, 4), "valid_fraction": round(valid, 4),
+                     "stage_ms": {"transform": round(st[0], 4), "search": round(st[1], 4),
+                                  "agreement": round(st[2], 4)},
+                     "stage_rooflines": stage_rooflines(st, rows, cols, n, clk, valid, eb=2, nwords=12, dirs=2,
+                                                        full=True,
+                                                        agree="subpixel_f64" if form == 0 else "moments")}
+    (d_ref, c_ref), (d_mom, c_mom) = outs["reference_form"], outs["moment_form"]
+    res["moment_form_error_vs_fp64_reference"] = moment_form_error(d_ref, c_ref, d_mom, c_mom)
+    return c0, res
 
 
 def learned_error(lbg, pybicos, left, right, plain, learned, n):
@@ -357,9 +457,12 @@ def run_ours(args):
     def timed(double, steps, warmup, stage_times=False, form=0):
         cfg = cfg_of(double)
         cfg.nxcorr_form = form
-        out = lbg.match_device(left, right, cfg)
+        return timed_match(left, right, cfg, steps, warmup, stage_times)
+
+    def timed_match(left, right, cfg, steps, warmup, stage_times=False, max_bits=256):
+        out = lbg.match_device(left, right, cfg, max_bits=max_bits)
         for _ in range(warmup):
-            lbg.match_device(left, right, cfg, out=out)
+            lbg.match_device(left, right, cfg, out=out, max_bits=max_bits)
         stream = torch.cuda.current_stream()
         if stage_times:
             N.check(L.bicos_stage_timing(1))
@@ -368,7 +471,7 @@ def run_ours(args):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(steps):
-            lbg.match_device(left, right, cfg, out=out)
+            lbg.match_device(left, right, cfg, out=out, max_bits=max_bits)
         e1.record(stream)
         torch.cuda.synchronize()
         barrier()
@@ -402,7 +505,7 @@ def run_ours(args):
         "valid_fraction": round(valid, 4),
     }
     result["stage_ms"] = {"transform": round(stages[0], 4), "search": round(stages[1], 4),
-                          "agree_subpixel": round(stages[2], 4)}
+                          "agreement": round(stages[2], 4)}
     result["gpu_launches"] = 3 * args.steps
 
     # per-stage rooflines; the headline one is the stage that takes longest
@@ -415,14 +518,20 @@ def run_ours(args):
         result["double"] = {"value": round(ws * px / (ms_d * 1e-3) / 1e6, 3), "unit": "Mpx/s",
                             "ms_per_step": round(ms_d, 4),
                             "stage_ms": {"transform": round(st_d[0], 4), "search": round(st_d[1], 4),
-                                         "agree_subpixel": round(st_d[2], 4)}}
+                                         "agreement": round(st_d[2], 4)},
+                            "stage_rooflines": stage_rooflines(st_d, rows, cols, n, clk, valid,
+                                                               agree="subpixel_f64")}
         # the moment form (extension): exact integer moments, Sxy on the
         # tensor cores, closed-form sweep of the unrounded interpolant, FP64
         ms_m, st_m, _ = timed(True, max(1, args.steps // 2), 2, stage_times=True, form=1)
         result["moment_form_double"] = {
             "value": round(ws * px / (ms_m * 1e-3) / 1e6, 3), "unit": "Mpx/s", "ms_per_step": round(ms_m, 4),
             "stage_ms": {"transform": round(st_m[0], 4), "search": round(st_m[1], 4),
-                         "agree_subpixel": round(st_m[2], 4)}}
+                         "agreement": round(st_m[2], 4)}}
+
+    if not args.no_configs and ws == 1:
+        result["c0_vga"], result["c2_precision"] = config_benches(lbg, pybicos, scenes, timed_match, clk,
+                                                                  args.seed, max(5, args.steps // 2))
 
     if not args.no_learned and N.load().bicos_learned_model_installed():
         # the learned subpixel form (extension): network proposal, one
@@ -504,12 +613,16 @@ def run_reference(args):
     value = rows * scene.left.shape[2] / dt / 1e6
     cores = os.cpu_count() if use_ref else O.lib().orc_num_threads(0)
     kind = "reference" if use_ref else "port"
-    sample = f"rows 0..{rows - 1} of the {WORKLOAD} stack (all columns, n=33) per step"
+    sample = f"rows 0..{rows - 1} of the {WORKLOAD} stack (all columns, n=33) per step" + \
+        ("" if use_ref else f"; {PORT_VS_REFERENCE}")
+    config = dict(workload_config(False),
+                  sample=f"each step matches rows 0..{rows - 1} ({rows} of 1216 rows, all 1936 columns) of the "
+                         f"stack on the host cores; Mpx/s = the sample's pixels / its time")
     print(json.dumps({
         "metric": METRIC, "value": round(value, 4), "unit": "Mpx/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(dt * 1e3, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u8", "data": f"synthetic (seeded scene, seed {args.seed})",
-        "config": workload_config(False), "impl": "reference",
+        "config": config, "impl": "reference",
         "cpu_baseline": {"value": round(value, 4), "unit": "Mpx/s", "cores": cores, "kind": kind, "sample": sample},
         "e2e": {"value": round(value, 4), "unit": "Mpx/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)

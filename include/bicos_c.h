@@ -214,8 +214,10 @@ bicos_status bicos_search_bits_v1(const uint32_t* desc0, const uint32_t* desc1, 
  * (limit rows * cols <= 4194304 pixels, larger sizes fail with
  * BICOS_ERR_INVALID_ARGUMENT), held by every GPU that loads it until the
  * process exits.  The first call on a device looks up the array's device
- * address (cudaGetSymbolAddress) with that device current; make that first
- * call before any stream capture.  All calls share the array: calls that
+ * address (cudaGetSymbolAddress) with that device current, which under
+ * lazy module loading also loads the array: make one consistency call at
+ * initialisation, outside any stream capture (a failed lookup is retried on
+ * the next call).  All calls share the array: calls that
  * overlap on the GPU race, so serialise them.  Without the consistency flag
  * no scratch is used.  Outputs equal bicos_search_v1's.
  */
@@ -260,6 +262,10 @@ int32_t bicos_png_unfilter(uint8_t* out, const uint8_t* raw, int32_t height, siz
  * after all pushes, on `stream`; outputs as bicos_match_v1.  A handle is
  * used by one host thread at a time; the frames stay resident, so a stack
  * can be matched again (another configuration) without new pushes.
+ * Ordering across streams is handled by the handle: matches of one handle
+ * run in call order, and a push is ordered after every earlier match, so a
+ * capture thread may push the next stack on its upload stream while the
+ * previous match still runs on a compute stream.
  */
 typedef struct bicos_ingest bicos_ingest;
 bicos_status bicos_ingest_create(bicos_ingest** out, int32_t rows, int32_t cols, uint32_t n, int32_t type);
@@ -300,8 +306,10 @@ bicos_status bicos_agree_subpixel_v1(const bicos_image* raw_disparity, const bic
  *   stream completes, the number of pixels that fell back to the sweep.
  * bicos_learned_model_v1: installs a model file image ("BICOSMLP" version
  *   1: header, FP32 input statistics, BF16 parameters) for this process,
- *   replacing the built-in one; NULL uninstalls.  Not to be called while
- *   matches in the learned form are in flight.
+ *   replacing the built-in one; NULL uninstalls.  The next learned-form
+ *   call on each device uploads it, after synchronising that device when a
+ *   previous model is in its buffer (work still in flight, on any stream or
+ *   in a cached batch graph, finishes with the model it started with).
  * bicos_mlp_*: the network's own training kernels on device buffers (model
  *   layout: parameters, then 7 input means and 7 standard deviations;
  *   samples: 8 floats, the feature row with the target offset in the last

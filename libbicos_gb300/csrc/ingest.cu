@@ -25,6 +25,10 @@ struct bicos_ingest {
     void* frames = nullptr;
     std::vector<cudaEvent_t> done;  // frame t of both sides uploaded
     std::vector<char> pushed;
+    // recorded after the last match's kernels on the match's stream: a push
+    // waits for it before overwriting a frame that match may still read
+    cudaEvent_t consumed = nullptr;
+    bool matched = false;
 };
 
 namespace {
@@ -69,6 +73,8 @@ bicos_status bicos_ingest_create(bicos_ingest** out, int32_t rows, int32_t cols,
     cudaError_t e = cudaMalloc(&h->frames, 2 * (size_t)n * h->plane);
     for (uint32_t t = 0; t < n && e == cudaSuccess; ++t)
         e = cudaEventCreateWithFlags(&h->done[t], cudaEventDisableTiming);
+    if (e == cudaSuccess)
+        e = cudaEventCreateWithFlags(&h->consumed, cudaEventDisableTiming);
     if (e != cudaSuccess) {
         bicos_ingest_destroy(h);
         return ingest_cuda_fail(e, "bicos_ingest_create");
@@ -83,6 +89,8 @@ bicos_status bicos_ingest_destroy(bicos_ingest* h) {
     for (cudaEvent_t ev : h->done)
         if (ev)
             cudaEventDestroy(ev);
+    if (h->consumed)
+        cudaEventDestroy(h->consumed);
     if (h->frames)
         cudaFree(h->frames);
     delete h;
@@ -100,7 +108,9 @@ bicos_status bicos_ingest_push_v1(bicos_ingest* h, uint32_t t, const void* frame
         return ingest_fail(BICOS_ERR_INVALID_ARGUMENT, "host row step smaller than a row");
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     char* base = static_cast<char*>(h->frames);
-    cudaError_t e = cudaSuccess;
+    // write-after-read: the previous match (possibly on another stream) may
+    // still be reading this frame
+    cudaError_t e = h->matched ? cudaStreamWaitEvent(st, h->consumed, 0) : cudaSuccess;
     for (int side = 0; side < 2 && e == cudaSuccess; ++side) {
         char* dst = base + ((size_t)side * h->n + t) * h->plane;
         const void* src = side ? frame1 : frame0;
@@ -128,13 +138,24 @@ bicos_status bicos_ingest_match_v1(bicos_ingest* h, bicos_image* disparity, bico
     for (uint32_t t = 0; t < h->n; ++t)  // pushes may have used other streams
         if (cudaError_t e = cudaStreamWaitEvent(st, h->done[t], 0))
             return ingest_cuda_fail(e, "bicos_ingest_match_v1");
+    // matches of one handle run in call order, so the event recorded after
+    // this one also covers every earlier match (whatever its stream)
+    if (h->matched)
+        if (cudaError_t e = cudaStreamWaitEvent(st, h->consumed, 0))
+            return ingest_cuda_fail(e, "bicos_ingest_match_v1");
     bicos_image im0[kMaxFrames], im1[kMaxFrames];
     char* base = static_cast<char*>(h->frames);
     for (uint32_t t = 0; t < h->n; ++t) {
         im0[t] = bicos_image{base + (size_t)t * h->plane, h->row_bytes, h->rows, h->cols, h->type, 0};
         im1[t] = bicos_image{base + ((size_t)h->n + t) * h->plane, h->row_bytes, h->rows, h->cols, h->type, 0};
     }
-    return bicos_match_v1(im0, im1, h->n, disparity, corrmap, cfg, stream);
+    const bicos_status s = bicos_match_v1(im0, im1, h->n, disparity, corrmap, cfg, stream);
+    if (s != BICOS_OK)
+        return s;
+    if (cudaError_t e = cudaEventRecord(h->consumed, st))
+        return ingest_cuda_fail(e, "bicos_ingest_match_v1");
+    h->matched = true;
+    return BICOS_OK;
 }
 
 }  // extern "C"

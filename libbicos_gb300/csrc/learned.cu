@@ -1066,7 +1066,14 @@ const float* learned_model_device(cudaStream_t st, std::string* err) {
     if (e == cudaSuccess && !dm.ptr)
         e = cudaMalloc(&dm.ptr, kModelFloats * sizeof(float));
     if (e == cudaSuccess && dm.version != g_model_version) {
-        e = cudaMemcpyAsync(dm.ptr, g_model.data(), kModelFloats * sizeof(float), cudaMemcpyHostToDevice, st);
+        // a model install replaced the one this buffer holds: kernels (or a
+        // cached batch graph) still running on other streams may read it,
+        // so the device finishes its work before the buffer is rewritten
+        // (installs are rare)
+        if (dm.version != 0)
+            e = cudaDeviceSynchronize();
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(dm.ptr, g_model.data(), kModelFloats * sizeof(float), cudaMemcpyHostToDevice, st);
         if (e == cudaSuccess)
             e = cudaStreamSynchronize(st);
         if (e == cudaSuccess)

@@ -15,9 +15,14 @@
 // GPU that loads this part of the library holds the array until the
 // process exits.  No element needs clearing between calls: the search
 // kernel writes every best column of the image before the combine kernel
-// reads any of them.  All calls share the one array, so calls whose work
-// overlaps on the GPU (different streams, or threads without ordering)
-// race on it; serialise them.
+// reads any of them (a search CTA whose bounded waits run out writes -1,
+// "no match", for its pixels instead of leaving the previous call's
+// columns).  All calls share the one array, so calls whose work overlaps
+// on the GPU (different streams, or threads without ordering) race on it;
+// serialise them.  The first consistency call on a device looks the
+// array's address up, which also loads the module holding it where modules
+// load lazily: make one such call at initialisation, outside any stream
+// capture, so that later calls only launch kernels.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -34,15 +39,14 @@ static __device__ __align__(256) int32_t g_noalloc_best[2 * kNoAllocMaxPixels];
 
 constexpr int kMaxDevices = 64;
 
-struct DeviceScratch {
-    std::once_flag once;
-    int32_t* ptr = nullptr;
-    cudaError_t err = cudaSuccess;
-};
-DeviceScratch g_device_scratch[kMaxDevices];
+std::mutex g_scratch_mu;
+int32_t* g_scratch_ptr[kMaxDevices] = {};
 
-// Device address of the array on the current device, looked up once per
-// device (in host code the array's name is only a host-side stand-in).
+// Device address of the array on the current device (in host code the
+// array's name is only a host-side stand-in).  Only a successful lookup is
+// kept: a lookup that failed (for instance one attempted inside a stream
+// capture, where loading the module holding the array is not allowed) is
+// tried again on the next call.
 cudaError_t scratch_address(int32_t** out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -50,15 +54,15 @@ cudaError_t scratch_address(int32_t** out) {
         return e;
     if (dev < 0 || dev >= kMaxDevices)
         return cudaErrorInvalidDevice;
-    DeviceScratch& d = g_device_scratch[dev];
-    std::call_once(d.once, [&d] {
+    std::lock_guard<std::mutex> lk(g_scratch_mu);
+    if (!g_scratch_ptr[dev]) {
         void* p = nullptr;
-        d.err = cudaGetSymbolAddress(&p, g_noalloc_best);
-        d.ptr = static_cast<int32_t*>(p);
-    });
-    if (d.err != cudaSuccess)
-        return d.err;
-    *out = d.ptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_best);
+        if (e != cudaSuccess)
+            return e;
+        g_scratch_ptr[dev] = static_cast<int32_t*>(p);
+    }
+    *out = g_scratch_ptr[dev];
     return cudaSuccess;
 }
 

@@ -407,7 +407,15 @@ __global__ void __launch_bounds__(kThreadsTC, 2) k_search_tc(const uint32_t* __r
         }
         asm volatile("bar.sync 1, %0;" ::"r"(32 * kEpiWarps) : "memory");
         const int c = m0 + q * 32 + lane;
-        if (half == 0 && !*abort && c < cols) {
+        if (half == 0 && *abort && c < cols) {
+            // the CTA gave up: no match rather than stale outputs
+            if (disp) {
+                int16_t* o = reinterpret_cast<int16_t*>(reinterpret_cast<char*>(disp) + row * disp_pitch);
+                o[c] = kInvalidDisp;
+            } else {
+                (dir ? best1 : best0)[(size_t)row * cols + c] = -1;
+            }
+        } else if (half == 0 && c < cols) {
             const float2 r = sh.red[q * 32 + lane];
             int best;
             bool valid;

@@ -181,21 +181,62 @@ static inline int ham(const uint32_t* a, const uint32_t* b, int nwords) {
     return s;
 }
 
-static int bicos_search(const uint32_t* d0, const uint32_t* row1, int cols, int nwords, int flags) {
-    int best = INVALID_INT, min_cost = INT_MAX, dups = 0;
-    for (int c1 = 0; c1 < cols; ++c1) {
-        const int cost = ham(d0, row1 + (size_t)c1 * nwords, nwords);
-        if (cost < min_cost) {
-            min_cost = cost;
-            best = c1;
-            if (flags & ORC_FLAG_NODUPES)
-                dups = 0;
-        } else if ((flags & ORC_FLAG_NODUPES) && cost == min_cost)
-            dups++;
+/* 64-bit popcounts over pairs of words (the reference's u64/u128 words,
+ * include/impl/cpu/bicos.hpp:29-48); same counts as ham() */
+static inline int ham64(const uint32_t* a, const uint32_t* b, int npairs) {
+    int s = 0;
+    for (int k = 0; k < npairs; ++k) {
+        uint64_t x, y;
+        memcpy(&x, a + 2 * k, 8);
+        memcpy(&y, b + 2 * k, 8);
+        s += __builtin_popcountll(x ^ y);
     }
-    if ((flags & ORC_FLAG_NODUPES) && dups > 0)
-        return INVALID_INT;
+    return s;
+}
+
+/* include/impl/cpu/bicos.hpp:50-76; one body per descriptor width so the
+ * word loop is unrolled (the reference's template on the descriptor type) */
+#define ORC_SEARCH_BODY(COST)                                                \
+    int best = INVALID_INT, min_cost = INT_MAX, dups = 0;                  \
+    for (int c1 = 0; c1 < cols; ++c1) {                                    \
+        const uint32_t* cand = row1 + (size_t)c1 * nwords;                 \
+        const int cost = (COST);                                           \
+        if (cost < min_cost) {                                             \
+            min_cost = cost;                                               \
+            best = c1;                                                     \
+            if (flags & ORC_FLAG_NODUPES)                                  \
+                dups = 0;                                                  \
+        } else if ((flags & ORC_FLAG_NODUPES) && cost == min_cost)         \
+            dups++;                                                        \
+    }                                                                      \
+    if ((flags & ORC_FLAG_NODUPES) && dups > 0)                            \
+        return INVALID_INT;                                                \
     return best;
+
+#define ORC_SEARCH_NW(NAME, NPAIRS)                                                       \
+    static int NAME(const uint32_t* d0, const uint32_t* row1, int cols, int flags) {     \
+        const int nwords = 2 * (NPAIRS);                                                  \
+        ORC_SEARCH_BODY(ham64(d0, cand, NPAIRS))                                          \
+    }
+ORC_SEARCH_NW(search_w2, 1)
+ORC_SEARCH_NW(search_w4, 2)
+ORC_SEARCH_NW(search_w8, 4)
+ORC_SEARCH_NW(search_w12, 6)
+ORC_SEARCH_NW(search_w16, 8)
+
+static int search_any(const uint32_t* d0, const uint32_t* row1, int cols, int nwords, int flags) {
+    ORC_SEARCH_BODY(ham(d0, cand, nwords))
+}
+
+static int bicos_search(const uint32_t* d0, const uint32_t* row1, int cols, int nwords, int flags) {
+    switch (nwords) {
+        case 2: return search_w2(d0, row1, cols, flags);
+        case 4: return search_w4(d0, row1, cols, flags);
+        case 8: return search_w8(d0, row1, cols, flags);
+        case 12: return search_w12(d0, row1, cols, flags);
+        case 16: return search_w16(d0, row1, cols, flags);
+        default: return search_any(d0, row1, cols, nwords, flags);
+    }
 }
 
 typedef struct {

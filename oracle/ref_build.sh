@@ -3,11 +3,12 @@
 # against the project's minimal OpenCV/fmt stand-in (oracle/ref_shim) into
 # oracle/_ref/libbicos_ref.so.  TEST INFRASTRUCTURE ONLY: the result is the
 # checker that pins the oracle restatement and generates tests/golden/.
-# Needs the reference sources at $BICOS_REF (default /root/reference); exits
-# 0 without building when they are absent.
+# Needs the reference sources at $BICOS_REF (default: a libBICOS tree named
+# "reference" beside this repository's checkout); exits 0 without building
+# when they are absent.
 set -e
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF="${BICOS_REF:-/root/reference}"
+REF="${BICOS_REF:-$HERE/../../reference}"
 if [ ! -f "$REF/src/impl/cpu.cpp" ]; then
     echo "ref_build: reference sources not found at $REF, skipping" >&2
     exit 0

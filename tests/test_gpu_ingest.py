@@ -60,3 +60,35 @@ def test_ingest_errors_and_replacement(cuda):
     d, _ = ing.match(_cfg())
     wd, _ = lbg.match_device(dev(other.left, cuda), dev(other.right, cuda), _cfg())
     assert_same(host(d), host(wd))
+
+
+def test_push_on_another_stream_after_match(cuda):
+    """a capture thread pushes the next stack on its upload stream while the
+    previous match still runs on a compute stream: the handle orders each
+    push after the earlier matches, so both matches see their own stack"""
+    a = scenes.make_scene(512, 1024, 12, seed=30)
+    b = scenes.make_scene(512, 1024, 12, seed=31)
+    pin = lambda x: torch.from_numpy(np.ascontiguousarray(x)).pin_memory()
+    frames_b = [(pin(b.left[t]), pin(b.right[t])) for t in range(12)]
+    compute, upload = torch.cuda.Stream(), torch.cuda.Stream()
+    ing = lbg.Ingest(512, 1024, 12)
+    for t in range(12):
+        ing.push(t, a.left[t], a.right[t], stream=compute)
+    torch.cuda.synchronize()
+    for _ in range(3):
+        with torch.cuda.stream(compute):
+            da, ca = ing.match(_cfg(0.1), stream=compute)
+        for t in range(12):  # no host synchronisation in between
+            ing.push(t, frames_b[t][0], frames_b[t][1], stream=upload)
+        with torch.cuda.stream(upload):
+            db, cb = ing.match(_cfg(0.1), stream=upload)
+        torch.cuda.synchronize()
+        wa, wca = lbg.match_device(dev(a.left, cuda), dev(a.right, cuda), _cfg(0.1))
+        wb, wcb = lbg.match_device(dev(b.left, cuda), dev(b.right, cuda), _cfg(0.1))
+        assert_same(host(da), host(wa), "stack a")
+        assert_same(host(ca), host(wca), "stack a corr")
+        assert_same(host(db), host(wb), "stack b")
+        assert_same(host(cb), host(wcb), "stack b corr")
+        for t in range(12):
+            ing.push(t, a.left[t], a.right[t], stream=compute)
+    ing.close()
