@@ -241,6 +241,20 @@ bicos_status bicos_search_noalloc_v1(const uint32_t* desc0, const uint32_t* desc
 bicos_status bicos_reproject_v1(const bicos_image* disparity, const double* q, bicos_image* points,
                                 bicos_stream_t stream);
 
+/*
+ * bicos_match_v1 plus the point cloud of its disparity in the same pass:
+ * the match bicos-cli runs followed by its cv::reprojectImageTo3D step
+ * (src/cli.cpp:188-194, 228-250).  Arguments and outputs as
+ * bicos_match_v1; q and points as bicos_reproject_v1, whose points this
+ * writes bit for bit.  With the reference NCC form and a threshold, the
+ * agreement kernel writes each pixel's point as it writes its disparity
+ * (no second pass over HBM); without a threshold, or in the MOMENTS and
+ * LEARNED forms, the reprojection pass runs after the match on `stream`.
+ */
+bicos_status bicos_match_points_v1(const bicos_image* stack0, const bicos_image* stack1, uint32_t n,
+                                   bicos_image* disparity, bicos_image* corrmap, const bicos_config* cfg,
+                                   const double* q, bicos_image* points, bicos_stream_t stream);
+
 /* Host utility of the command-line front end (no GPU work): reconstructs
  * `height` PNG scanlines of `stride` bytes from the inflated image data
  * `raw` (each row: one filter byte, then stride bytes; ISO/IEC 15948

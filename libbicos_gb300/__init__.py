@@ -59,13 +59,17 @@ def _raise(st):
 
 
 def match_device(stack0, stack1, cfg: Config | None = None, stream=None, out=None, corrmap=True,
-                 max_bits: int = 256):
-    """BICOS::match on CUDA tensors.  Returns (disparity, corrmap or None).
+                 max_bits: int = 256, q=None, points=None):
+    """BICOS::match on CUDA tensors.  Returns (disparity, corrmap or None),
+    or (disparity, corrmap, points) when a reprojection matrix ``q`` (4x4)
+    is given.
 
     stack0/stack1: (n, rows, cols) uint8/uint16 CUDA tensors or lists of
-    2-D ones.  ``out`` may supply (disparity, corrmap) tensors to reuse.
-    Enqueued on ``stream`` (torch's current stream by default); returns
-    without synchronising.
+    2-D ones.  ``out`` may supply (disparity, corrmap) tensors to reuse and
+    ``points`` a (rows, cols, 3) float32 tensor.  With ``q`` the point cloud
+    is written in the same pass (bicos_match_points_v1).  Enqueued on
+    ``stream`` (torch's current stream by default); returns without
+    synchronising.
     """
     import torch
     cfg = Config() if cfg is None else cfg
@@ -89,10 +93,21 @@ def match_device(stack0, stack1, cfg: Config | None = None, stream=None, out=Non
                                device=f0.device)
     di = N.tensor_image(disp)
     ci = N.tensor_image(corr) if corr is not None else None
-    st = N.load().bicos_match_v1(a0, a1, n, C.byref(di), C.byref(ci) if ci is not None else None,
-                                 C.byref(nc), _stream_ptr(stream))
+    if q is None:
+        st = N.load().bicos_match_v1(a0, a1, n, C.byref(di), C.byref(ci) if ci is not None else None,
+                                     C.byref(nc), _stream_ptr(stream))
+        _raise(st)
+        return disp, corr
+    import numpy as np
+    qa = np.ascontiguousarray(np.asarray(q, dtype=np.float64).reshape(4, 4))
+    if points is None:
+        points = torch.empty((rows, cols, 3), dtype=torch.float32, device=f0.device)
+    pi = N.points_image(points)
+    st = N.load().bicos_match_points_v1(a0, a1, n, C.byref(di), C.byref(ci) if ci is not None else None,
+                                        C.byref(nc), qa.ctypes.data_as(C.POINTER(C.c_double)), C.byref(pi),
+                                        _stream_ptr(stream))
     _raise(st)
-    return disp, corr
+    return disp, corr, points
 
 
 def descriptor_transform(stack, full: bool, stream=None):

@@ -88,6 +88,7 @@ def load():
         "bicos_search_v1": ([P, P, I, I, U, I, I, IMG, P], C.c_int),
         "bicos_search_bits_v1": ([P, P, I, I, U, I, I, I, IMG, P], C.c_int),
         "bicos_reproject_v1": ([IMG, C.POINTER(C.c_double), IMG, P], C.c_int),
+        "bicos_match_points_v1": ([IMG, IMG, U, IMG, IMG, CFG, C.POINTER(C.c_double), IMG, P], C.c_int),
         "bicos_png_unfilter": ([P, P, C.c_int32, S, C.c_int32], C.c_int32),
         "bicos_ingest_create": ([C.POINTER(P), I, I, U, I], C.c_int),
         "bicos_ingest_destroy": ([P], C.c_int),

@@ -138,12 +138,14 @@ __device__ __forceinline__ void agree_block_body(const AgreeParams& p, int bx, i
     const int16_t d = *dp;
     if (d == kInvalidDisp) {
         put_corr<TP>(p, row, col, (TP)NAN);
+        agree_point(p, row, col, (float)kInvalidDisp);
         return;
     }
     const int col1 = col - d;
     if (col1 < 0 || cols <= col1) {
         *dp = kInvalidDisp;
         put_corr<TP>(p, row, col, (TP)NAN);
+        agree_point(p, row, col, (float)kInvalidDisp);
         return;
     }
     int x[NMAX], y[NMAX];
@@ -154,8 +156,10 @@ __device__ __forceinline__ void agree_block_body(const AgreeParams& p, int bx, i
     }
     const TP nxc = nxc_full<DBL>(x, y, n, p.has_minvar != 0, p.minvar);
     put_corr<TP>(p, row, col, nxc);
-    if (nxc < (TP)p.thr)
+    const bool keep = !(nxc < (TP)p.thr);
+    if (!keep)
         *dp = kInvalidDisp;
+    agree_point(p, row, col, keep ? (float)d : (float)kInvalidDisp);
 }
 
 template<typename T, bool DBL, int NMAX>
@@ -544,6 +548,7 @@ __device__ __forceinline__ void subpixel_f32_body(const AgreeParams& p, int bx, 
     }
     reinterpret_cast<float*>(reinterpret_cast<char*>(p.out) + row * p.out_pitch)[col] = result;
     put_corr<float>(p, row, col, corr);
+    agree_point(p, row, col, result);
 }
 
 template<typename T, int NMAX>
@@ -779,6 +784,7 @@ __device__ __forceinline__ void subpixel_f64_body(const AgreeParams& p, int bx, 
     }
     reinterpret_cast<float*>(reinterpret_cast<char*>(p.out) + row * p.out_pitch)[col] = result;
     put_corr<double>(p, row, col, corr);
+    agree_point(p, row, col, result);
 }
 
 template<typename T, int NMAX>

@@ -283,7 +283,7 @@ void bicos_gb300::set_last_error(const std::string& msg) { g_last_error = msg; }
 // ---- one match: validation, scratch layout, stages (also used by the batch API)
 
 size_t MatchPlan::scratch_bytes() const {
-    return 2 * desc_bytes + raw_bytes + 2 * best_bytes + learned_bytes;
+    return 2 * desc_bytes + raw_bytes + 2 * best_bytes + learned_bytes + expand_bytes;
 }
 
 bicos_status bicos_gb300::plan_match(const bicos_image* stack0, const bicos_image* stack1, uint32_t n,
@@ -331,6 +331,7 @@ bicos_status bicos_gb300::plan_match(const bicos_image* stack0, const bicos_imag
     P.raw_bytes = P.sub ? align_up(px * 2, 256) : 0;
     P.best_bytes = P.consistency ? align_up(px * 4, 256) : 0;
     P.learned_bytes = P.learned ? learned_scratch_bytes(px) : 0;
+    P.expand_bytes = align_up(search_expand_bytes(P.rows, P.cols, P.nw, P.consistency ? 2 : 1), 256);
     return BICOS_OK;
 }
 
@@ -344,6 +345,9 @@ MatchBuffers bicos_gb300::match_buffers(const MatchPlan& P, void* scratch) {
     m.fwd = P.consistency ? reinterpret_cast<int32_t*>(b + 2 * P.desc_bytes + P.raw_bytes) : nullptr;
     m.rev = P.consistency ? reinterpret_cast<int32_t*>(b + 2 * P.desc_bytes + P.raw_bytes + P.best_bytes) : nullptr;
     m.learned = P.learned ? b + 2 * P.desc_bytes + P.raw_bytes + 2 * P.best_bytes : nullptr;
+    m.expand = P.expand_bytes
+                   ? reinterpret_cast<uint8_t*>(b + 2 * P.desc_bytes + P.raw_bytes + 2 * P.best_bytes + P.learned_bytes)
+                   : nullptr;
     return m;
 }
 
@@ -355,13 +359,13 @@ cudaError_t bicos_gb300::enqueue_search(const MatchPlan& P, const MatchBuffers& 
     const int bits = descriptor_positions(P.n, P.full);
     if (P.consistency) {
         cudaError_t e = launch_search(m.d0, m.d1, P.rows, P.cols, P.nw, bits, P.cfg->no_dupes != 0, 2, nullptr, 0,
-                                      m.fwd, m.rev, st);
+                                      m.fwd, m.rev, st, m.expand);
         if (e == cudaSuccess)
             e = launch_consistency(m.fwd, m.rev, P.rows, P.cols, P.cfg->max_lr_diff, m.raw, m.raw_pitch, st);
         return e;
     }
     return launch_search(m.d0, m.d1, P.rows, P.cols, P.nw, bits, true, 1, m.raw, m.raw_pitch, nullptr, nullptr,
-                         st);
+                         st, m.expand);
 }
 
 AgreeParams bicos_gb300::agree_params(const MatchPlan& P, const MatchBuffers& m) {
@@ -386,11 +390,42 @@ AgreeParams bicos_gb300::agree_params(const MatchPlan& P, const MatchBuffers& m)
     return ap;
 }
 
+namespace {
+// the plan's point cloud from its finished disparity (a separate pass)
+cudaError_t reproject_after(const MatchPlan& P, cudaStream_t st) {
+    ReprojectParams rp;
+    rp.disp = P.disparity->data;
+    rp.disp_pitch = (long long)P.disparity->step;
+    rp.pts = P.pts;
+    rp.pts_pitch = P.pts_pitch;
+    rp.rows = P.rows;
+    rp.cols = P.cols;
+    for (int i = 0; i < 16; ++i)
+        rp.q[i] = P.q[i];
+    return launch_reproject(rp, P.disparity->type == BICOS_32F, st);
+}
+}  // namespace
+
 cudaError_t bicos_gb300::enqueue_agree(const MatchPlan& P, const MatchBuffers& m, const float* model,
                                        cudaStream_t st) {
     if (!P.thr)
-        return cudaSuccess;
-    const AgreeParams ap = agree_params(P, m);
+        return P.pts ? reproject_after(P, st) : cudaSuccess;
+    AgreeParams ap = agree_params(P, m);
+    if (P.pts && !P.moments && !P.learned) {  // fused: the agreement kernel writes the points
+        ap.pts = P.pts;
+        ap.pts_pitch = P.pts_pitch;
+        for (int i = 0; i < 16; ++i)
+            ap.q[i] = P.q[i];
+        return P.sub ? launch_agree_subpixel(ap, P.dbl, st) : launch_agree(ap, P.dbl, st);
+    }
+    cudaError_t e = enqueue_agree_form(P, m, ap, model, st);
+    if (e == cudaSuccess && P.pts)
+        e = reproject_after(P, st);
+    return e;
+}
+
+cudaError_t bicos_gb300::enqueue_agree_form(const MatchPlan& P, const MatchBuffers& m, const AgreeParams& ap,
+                                            const float* model, cudaStream_t st) {
     if (P.moments) {
         MomentParams mp;
         std::memset(&mp, 0, sizeof mp);
@@ -498,12 +533,12 @@ bicos_status bicos_release_scratch(void) {
     return BICOS_OK;
 }
 
-bicos_status bicos_match_v1(const bicos_image* stack0, const bicos_image* stack1, uint32_t n,
-                            bicos_image* disparity, bicos_image* corrmap, const bicos_config* cfg,
-                            bicos_stream_t stream) {
-    MatchPlan plan;
-    if (bicos_status s = plan_match(stack0, stack1, n, disparity, corrmap, cfg, &plan))
-        return s;
+}  // extern "C"
+
+namespace {
+
+// the three stages of a planned match on `stream`, scratch from the cache
+bicos_status run_plan(const MatchPlan& plan, bicos_stream_t stream) {
     DeviceGuard g;
     if (g.err != cudaSuccess)
         return cuda_fail(g.err, "cudaGetDevice");
@@ -541,6 +576,39 @@ bicos_status bicos_match_v1(const bicos_image* stack0, const bicos_image* stack1
     if (er != cudaSuccess)
         return cuda_fail(er, "cudaEventRecord");
     return BICOS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+bicos_status bicos_match_v1(const bicos_image* stack0, const bicos_image* stack1, uint32_t n,
+                            bicos_image* disparity, bicos_image* corrmap, const bicos_config* cfg,
+                            bicos_stream_t stream) {
+    MatchPlan plan;
+    if (bicos_status s = plan_match(stack0, stack1, n, disparity, corrmap, cfg, &plan))
+        return s;
+    return run_plan(plan, stream);
+}
+
+bicos_status bicos_match_points_v1(const bicos_image* stack0, const bicos_image* stack1, uint32_t n,
+                                   bicos_image* disparity, bicos_image* corrmap, const bicos_config* cfg,
+                                   const double* q, bicos_image* points, bicos_stream_t stream) {
+    if (!q || !points)
+        return fail(BICOS_ERR_INVALID_ARGUMENT, "null argument");
+    MatchPlan plan;
+    if (bicos_status s = plan_match(stack0, stack1, n, disparity, corrmap, cfg, &plan))
+        return s;
+    if (!image_ok(points, plan.rows, plan.cols, BICOS_32FC3))
+        return fail(BICOS_ERR_EXCEPTION, "points must be a three-channel float32 image of the stack's size");
+    for (int i = 0; i < 16; ++i) {
+        if (!std::isfinite(q[i]))
+            return fail(BICOS_ERR_INVALID_ARGUMENT, "Q must be finite");
+        plan.q[i] = (float)q[i];
+    }
+    plan.pts = static_cast<float*>(points->data);
+    plan.pts_pitch = (long long)points->step;
+    return run_plan(plan, stream);
 }
 
 // Host buffers in, host buffers out.  The image is processed in row bands
@@ -719,28 +787,35 @@ bicos_status search_stage(const uint32_t* desc0, const uint32_t* desc1, int32_t 
         return fail(BICOS_ERR_EXCEPTION, "disparity must be an int16 image of the descriptor size");
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     const bool nodup = (flags & BICOS_FLAG_NODUPES) != 0;
-    cudaError_t e;
-    if (flags & BICOS_FLAG_CONSISTENCY) {
-        DeviceGuard g;
-        if (g.err != cudaSuccess)
-            return cuda_fail(g.err, "cudaGetDevice");
-        Scratch& s = g_scratch[g.dev % kMaxDevices];
-        std::lock_guard<std::mutex> lk(s.mu);
-        const size_t bb = align_up((size_t)rows * cols * 4, 256);
-        void* base = nullptr;
-        BICOS_CUDA_TRY(scratch_acquire(s, 2 * bb, st, &base));
+    const bool cons = (flags & BICOS_FLAG_CONSISTENCY) != 0;
+    DeviceGuard g;
+    if (g.err != cudaSuccess)
+        return cuda_fail(g.err, "cudaGetDevice");
+    // scratch: consistency bests, then the FP8 candidate tiles
+    Scratch& s = g_scratch[g.dev % kMaxDevices];
+    std::lock_guard<std::mutex> lk(s.mu);
+    const size_t bb = cons ? align_up((size_t)rows * cols * 4, 256) : 0;
+    const size_t xb = align_up(search_expand_bytes(rows, cols, (int)nwords, cons ? 2 : 1), 256);
+    void* base = nullptr;
+    cudaError_t e = cudaSuccess;
+    if (bb + xb > 0)
+        BICOS_CUDA_TRY(scratch_acquire(s, 2 * bb + xb, st, &base));
+    uint8_t* xbuf = xb ? static_cast<uint8_t*>(base) + 2 * bb : nullptr;
+    if (cons) {
         int32_t* fwd = static_cast<int32_t*>(base);
         int32_t* rev = reinterpret_cast<int32_t*>(static_cast<char*>(base) + bb);
-        e = launch_search(desc0, desc1, rows, cols, (int)nwords, bits, nodup, 2, nullptr, 0, fwd, rev, st);
+        e = launch_search(desc0, desc1, rows, cols, (int)nwords, bits, nodup, 2, nullptr, 0, fwd, rev, st, xbuf);
         if (e == cudaSuccess)
             e = launch_consistency(fwd, rev, rows, cols, max_lr_diff, static_cast<int16_t*>(disparity->data),
                                    (long long)disparity->step, st);
+    } else {
+        e = launch_search(desc0, desc1, rows, cols, (int)nwords, bits, nodup, 1, static_cast<int16_t*>(disparity->data),
+                          (long long)disparity->step, nullptr, nullptr, st, xbuf);
+    }
+    if (bb + xb > 0) {
         cudaError_t er = scratch_release(s, st);
         if (e == cudaSuccess)
             e = er;
-    } else {
-        e = launch_search(desc0, desc1, rows, cols, (int)nwords, bits, nodup, 1, static_cast<int16_t*>(disparity->data),
-                          (long long)disparity->step, nullptr, nullptr, st);
     }
     if (e != cudaSuccess)
         return cuda_fail(e, "search launch");

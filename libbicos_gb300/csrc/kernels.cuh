@@ -40,7 +40,35 @@ struct AgreeParams {
     // 1.0, read at run time: the sweep's packed sums fma(t, one, u) must not
     // be folded with the product that made t, which a literal 1 would allow
     float one = 1.0f;
+    // optional point cloud written in the same pass (bicos_match_points_v1):
+    // BICOS_32FC3 rows, Q row-major as floats
+    float* pts = nullptr;
+    long long pts_pitch = 0;
+    float q[16] = {};
 };
+
+// Point of pixel (x, y) with disparity d: [X Y Z W]^T = Q [x y d 1]^T
+// written as (X/W, Y/W, Z/W), W = 0 giving (0, 0, 0) (cv::reprojectImageTo3D
+// as bicos-cli runs it, src/cli.cpp:228-250); FP32, each row of Q a fused
+// sum.  Shared by the reprojection pass and the agreement kernels' fused
+// output, so both give the same bits.
+__device__ __forceinline__ void reproject_store(const float* q, float* pts_row, int x, int y, float d) {
+    const float fx = (float)x, fy = (float)y;
+    float h[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+        h[i] = fmaf(q[4 * i], fx, fmaf(q[4 * i + 1], fy, fmaf(q[4 * i + 2], d, q[4 * i + 3])));
+    const float iw = h[3] != 0.0f ? 1.0f / h[3] : 0.0f;
+    float* out = pts_row + 3 * x;
+    out[0] = h[0] * iw;
+    out[1] = h[1] * iw;
+    out[2] = h[2] * iw;
+}
+__device__ __forceinline__ void agree_point(const AgreeParams& p, int row, int col, float d) {
+    if (p.pts)
+        reproject_store(p.q, reinterpret_cast<float*>(reinterpret_cast<char*>(p.pts) + (long long)row * p.pts_pitch),
+                        col, row, d);
+}
 
 // moment form of the NCC stage (moments.cu)
 struct MomentParams {
@@ -69,10 +97,16 @@ cudaError_t launch_transform(const StackParams& p, int sides, bool full, int nwo
 // writes int32 best columns (-1 = invalid) of each direction to best0/best1.
 // bits: the descriptors' bit count when known (the transform's), else 0
 // (every bit of the nwords words may be set).
+// xbuf (optional, search_expand_bytes(rows, cols, nwords, directions)
+// bytes): scratch for the candidate sides expanded to FP8 tiles once per
+// call, which the tensor-core search then moves into shared memory with
+// bulk copies; without it the search expands them in every CTA.
 cudaError_t launch_search(const uint32_t* desc0, const uint32_t* desc1, int rows, int cols,
                           int nwords, int bits, bool nodupes, int directions, int16_t* disp,
                           long long disp_pitch, int32_t* best0, int32_t* best1,
-                          cudaStream_t st);
+                          cudaStream_t st, uint8_t* xbuf = nullptr);
+// bytes of the optional expansion scratch (0: the search cannot use one)
+size_t search_expand_bytes(int rows, int cols, int nwords, int directions);
 
 // point-cloud reprojection (reproject.cu): q = Q row-major, as floats
 struct ReprojectParams {
@@ -90,7 +124,7 @@ cudaError_t launch_reproject(const ReprojectParams& p, bool float_disp, cudaStre
 bool search_tc_supported(int cols);
 cudaError_t launch_search_tc(const uint32_t* desc0, const uint32_t* desc1, int rows, int cols, int nwords,
                              int bits, bool nodupes, int directions, int16_t* disp, long long disp_pitch,
-                             int32_t* best0, int32_t* best1, cudaStream_t st);
+                             int32_t* best0, int32_t* best1, cudaStream_t st, uint8_t* xbuf = nullptr);
 // number of tensor-core search CTAs whose bounded waits ran out (synchronous)
 unsigned int read_tc_faults();
 

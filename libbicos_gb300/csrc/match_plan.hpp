@@ -21,9 +21,16 @@ struct MatchPlan {
     bool full = false, thr = false, sub = false, dbl = false, consistency = false;
     bool moments = false, learned = false;
     // scratch layout: descriptors of both sides, raw disparity (subpixel
-    // runs), consistency bests, the learned form's buffers
-    size_t desc_bytes = 0, raw_bytes = 0, best_bytes = 0, learned_bytes = 0;
+    // runs), consistency bests, the learned form's buffers, the search's
+    // FP8 candidate tiles
+    size_t desc_bytes = 0, raw_bytes = 0, best_bytes = 0, learned_bytes = 0, expand_bytes = 0;
     size_t scratch_bytes() const;
+    // optional point cloud (bicos_match_points_v1): written by the
+    // reference-form agreement kernels as they write the disparity, or by
+    // the reprojection pass after the match in every other case
+    float* pts = nullptr;
+    long long pts_pitch = 0;
+    float q[16] = {};
 };
 
 struct MatchBuffers {
@@ -34,6 +41,7 @@ struct MatchBuffers {
     int32_t* fwd;
     int32_t* rev;
     void* learned;
+    uint8_t* expand;  // null: the search expands its candidate tiles in every CTA
 };
 
 // the reference's validation (src/impl/cuda.cu.in:233-292) with its error
@@ -49,5 +57,8 @@ AgreeParams agree_params(const MatchPlan& plan, const MatchBuffers& m);
 // the agreement stage in the plan's form (model: the learned form's device
 // model, else unused)
 cudaError_t enqueue_agree(const MatchPlan& plan, const MatchBuffers& m, const float* model, cudaStream_t st);
+// the agreement kernels of the plan's form (no point cloud)
+cudaError_t enqueue_agree_form(const MatchPlan& plan, const MatchBuffers& m, const AgreeParams& ap,
+                               const float* model, cudaStream_t st);
 
 }  // namespace bicos_gb300

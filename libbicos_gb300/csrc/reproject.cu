@@ -7,7 +7,9 @@
 // NaN propagating); the point-cloud writer skips them.
 //
 // One thread per pixel, FP32 arithmetic (X, Y, Z, W as fused sums of the
-// Q terms): HBM-bound, 2 or 4 bytes in and 12 bytes out per pixel.
+// Q terms, reproject_store in kernels.cuh): HBM-bound, 2 or 4 bytes in and
+// 12 bytes out per pixel.  bicos_match_points_v1 writes the same points
+// from the agreement kernels' epilogue instead (no second pass).
 #include "kernels.cuh"
 
 namespace bicos_gb300 {
@@ -19,16 +21,8 @@ __global__ void __launch_bounds__(256) k_reproject(const __grid_constant__ Repro
     if (x >= p.cols)
         return;
     const D* drow = reinterpret_cast<const D*>(reinterpret_cast<const char*>(p.disp) + (long long)y * p.disp_pitch);
-    const float d = (float)drow[x], fx = (float)x, fy = (float)y;
-    float h[4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-        h[i] = fmaf(p.q[4 * i], fx, fmaf(p.q[4 * i + 1], fy, fmaf(p.q[4 * i + 2], d, p.q[4 * i + 3])));
-    const float iw = h[3] != 0.0f ? 1.0f / h[3] : 0.0f;
-    float* out = reinterpret_cast<float*>(reinterpret_cast<char*>(p.pts) + (long long)y * p.pts_pitch) + 3 * x;
-    out[0] = h[0] * iw;
-    out[1] = h[1] * iw;
-    out[2] = h[2] * iw;
+    reproject_store(p.q, reinterpret_cast<float*>(reinterpret_cast<char*>(p.pts) + (long long)y * p.pts_pitch), x, y,
+                    (float)drow[x]);
 }
 
 }  // namespace

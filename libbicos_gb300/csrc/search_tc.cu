@@ -176,9 +176,9 @@ __device__ __forceinline__ void reduce_chunk(const float (&v)[32], int j0, int l
 }
 
 // The same reduction over column-coded keys (D = 128 * dot' - c, c the
-// column within the tile pair): chain A is the plain maximum of D; chain B
-// (with no-duplicates) keeps max(D + 2c) = 128 * dot' + c.  c0: the
-// chunk's first c.  Per pair of candidates: 1 three-input maximum, plus
+// column within the tile pair, v[j] at c = c0 + j): chain A is the plain
+// maximum of D; chain B (with no-duplicates) keeps max(D + 2c) =
+// 128 * dot' + c.  Per pair of candidates: 1 three-input maximum, plus
 // (no-duplicates) 2 FADDs and 1 more maximum.
 template<bool NODUP, bool MASKED>
 __device__ __forceinline__ void reduce_chunk_coded(const float (&v)[32], int c0, int lim, float& kA, float& kB) {
@@ -209,47 +209,61 @@ __device__ __forceinline__ void reduce_chunk_coded(const float (&v)[32], int c0,
     }
 }
 
-// a tile pair's coded maxima -> global integer keys 8192 * e - j (chain A,
-// first column) and 8192 * e + j (chain B, last column), e = dot' / 2,
-// j = 256 * pair + c; merged into the running maxima
-template<bool NODUP>
-__device__ __forceinline__ void merge_pair(float& kA, float& kB, int pair, int& gA, int& gB) {
+// one tile pair's chain-A maximum (D = 256 e - c) -> global key
+// 8192 e - (256 * pair + c), merged into gA; chain B (D + 2c = 256 e + c)
+// -> 8192 e + (256 * pair + c) into gB
+__device__ __forceinline__ void decode_a(float& kA, int pair, int& gA) {
     if (kA > -INFINITY) {
         const int a = (int)kA;
         const int c = (-a) & 255;
         gA = max(gA, ((a + c) >> 8) * 8192 - (pair * 256 + c));
-        if constexpr (NODUP) {
-            const int b = (int)kB;
-            const int cb = b & 255;
-            gB = max(gB, ((b - cb) >> 8) * 8192 + (pair * 256 + cb));
-        }
     }
-    kA = kB = -INFINITY;
+    kA = -INFINITY;
+}
+__device__ __forceinline__ void decode_b(float& kB, int pair, int& gB) {
+    if (kB > -INFINITY) {
+        const int b = (int)kB;
+        const int c = b & 255;
+        gB = max(gB, ((b - c) >> 8) * 8192 + (pair * 256 + c));
+    }
+    kB = -INFINITY;
 }
 
 // Warp roles of the pipelined CTA (one CTA = one row x 128 query pixels;
 // the MMA and producer waits back off between polls, the epilogue's do not):
 //   warps 0..7   epilogue: warp w reads TMEM lane quarter w%4, columns
 //                [64*(w/4), 64*(w/4)+64) of each accumulator
-//   warps 8..11  producers: thread p expands candidate row p of each tile
-//                into the FP8 ring (and query row p into the A tile)
-//   warp 12      MMA issue (one lane)
-// A ring of smem B buffers (4 for words up to 128 bits, else 2) and two
-// TMEM accumulators (2 x 128 columns) let the producers run ahead of the
-// tensor core, which runs one tile ahead of the epilogue.
+//   producers    in-kernel form (4 warps): thread p expands candidate row p
+//                of each tile into the FP8 ring (and query row p into the
+//                A tile); pre-expanded form (1 warp): the warp expands the
+//                A tile, then one lane moves each candidate tile, already
+//                in FP8 in global memory (k_expand_tiles), into the ring
+//                with one bulk copy
+//   last warp    MMA issue (one lane)
+// A ring of smem B buffers and two TMEM accumulators (2 x 128 columns) let
+// the producers run ahead of the tensor core, which runs one tile ahead of
+// the epilogue.
 constexpr int kEpiWarps = 8;
-constexpr int kProdWarps = 4;
-constexpr int kThreadsTC = 32 * (kEpiWarps + kProdWarps + 1);
+template<bool PRE>
+__host__ __device__ constexpr int prod_warps() { return PRE ? 1 : 4; }
+template<bool PRE>
+__host__ __device__ constexpr int threads_tc() { return 32 * (kEpiWarps + prod_warps<PRE>() + 1); }
 constexpr int kAccCols = kRows;
 
-constexpr int kMaxStages = 4;
+constexpr int kMaxStages = 5;
 
-template<int NW>
-__host__ __device__ constexpr int b_stages() { return NW <= 4 ? 4 : 2; }
+// B ring depth: in-kernel expansion 4 (words up to 128 bits) or 2; bulk
+// copies from L2 have a longer latency to cover, so 5 tiles of 16 KB (two
+// CTAs per SM within the 228 KB) or, for wider words, as many as fit
+template<int NW, bool PRE>
+__host__ __device__ constexpr int b_stages() {
+    return PRE ? (NW <= 4 ? 5 : NW <= 8 ? 2 : 1) : (NW <= 4 ? 4 : 2);
+}
 
 struct TcShared {
-    uint64_t full_b[kMaxStages];   // producers -> MMA, 128 arrivals
+    uint64_t full_b[kMaxStages];   // producers -> MMA (128 arrivals, or 1 + transaction bytes)
     uint64_t b_empty[kMaxStages];  // MMA commit -> producers (slot read)
+    uint64_t a_full;               // pre-expanded form: A tile written (32 arrivals)
     uint64_t acc_full[2];   // MMA commit -> epilogue / producers
     uint64_t acc_empty[2];  // epilogue -> MMA, 256 arrivals
     uint32_t tmem;
@@ -257,16 +271,36 @@ struct TcShared {
     float2 red[kRows];      // second column half's (chain A, chain B) maxima per query
 };
 
-template<int NW, bool NODUP, bool ENC>
-__global__ void __launch_bounds__(kThreadsTC, 2) k_search_tc(const uint32_t* __restrict__ d0,
-                                                             const uint32_t* __restrict__ d1, int rows, int cols,
-                                                             int16_t* __restrict__ disp, long long disp_pitch,
-                                                             int32_t* __restrict__ best0,
-                                                             int32_t* __restrict__ best1) {
+// Candidate descriptors -> FP8 tiles in global memory, in the B ring's
+// shared-memory layout (tile t of row r at xt + (r * ntiles + t) * TILE),
+// with the candidate clear pattern and, in the column-coded form, the
+// column code; rows past the last column repeat it (the epilogue masks
+// them).  One CTA of 128 threads per tile; each warp stores 512
+// contiguous bytes per 16-byte K chunk.
+template<int NW, bool ENC>
+__global__ void __launch_bounds__(kRows) k_expand_tiles(const uint32_t* __restrict__ d, int cols, int ntiles,
+                                                         uint8_t* __restrict__ xt) {
+    constexpr int TILE = kRows * NW * 32;
+    const int t = blockIdx.x, row = blockIdx.y, p = threadIdx.x;
+    const int c = min(t * kRows + p, cols - 1);
+    const Desc<NW> v = load_desc<NW>(d + ((size_t)row * cols + c) * NW);
+    expand_desc<NW, ENC>(xt + ((size_t)row * ntiles + t) * TILE, p, v, ENC ? kClearCand : kClearPlain,
+                         ENC ? column_code((t & 1) * kRows + p) : 0u);
+}
+
+template<int NW, bool NODUP, bool ENC, bool PRE>
+__global__ void __launch_bounds__(threads_tc<PRE>(), 2) k_search_tc(const uint32_t* __restrict__ d0,
+                                                                   const uint32_t* __restrict__ d1, int rows, int cols,
+                                                                   int16_t* __restrict__ disp, long long disp_pitch,
+                                                                   int32_t* __restrict__ best0,
+                                                                   int32_t* __restrict__ best1,
+                                                                   const uint8_t* __restrict__ x0,
+                                                                   const uint8_t* __restrict__ x1) {
     constexpr int KB = NW * 32;       // FP8 elements (bytes) per descriptor
     constexpr int TILE = kRows * KB;  // bytes of one 128-row tile
     constexpr int KSTEPS = KB / 32;   // MMA K = 32 bytes per instruction
-    constexpr int STAGES = b_stages<NW>();
+    constexpr int STAGES = b_stages<NW, PRE>();
+    constexpr int PROD = prod_warps<PRE>();
     extern __shared__ __align__(1024) uint8_t smem[];
     uint8_t* sA = smem;
     uint8_t* sB = smem + TILE;  // STAGES buffers
@@ -287,9 +321,10 @@ __global__ void __launch_bounds__(kThreadsTC, 2) k_search_tc(const uint32_t* __r
     }
     if (tid == 0) {
         for (int s = 0; s < STAGES; ++s) {
-            mbar_init(smem_u32(&sh.full_b[s]), 32 * kProdWarps);
+            mbar_init(smem_u32(&sh.full_b[s]), PRE ? 1 : 32 * PROD);
             mbar_init(smem_u32(&sh.b_empty[s]), 1);
         }
+        mbar_init(smem_u32(&sh.a_full), 32 * PROD);
         for (int b = 0; b < 2; ++b) {
             mbar_init(smem_u32(&sh.acc_full[b]), 1);
             mbar_init(smem_u32(&sh.acc_empty[b]), 32 * kEpiWarps);
@@ -301,12 +336,13 @@ __global__ void __launch_bounds__(kThreadsTC, 2) k_search_tc(const uint32_t* __r
     fence_after();
     const uint32_t tmem = sh.tmem;
 
-    if (warp >= kEpiWarps + kProdWarps) {
+    if (warp >= kEpiWarps + PROD) {
         // ---- MMA issue ----
         if (lane == 0) {
             const uint32_t a_addr = smem_u32(sA);
             int issued = -1;
-            for (int t = 0; t < ntiles; ++t) {
+            const bool a_ok = !PRE || wait_or_abort<32>(smem_u32(&sh.a_full), 0, abort);
+            for (int t = 0; t < ntiles && a_ok; ++t) {
                 const int b = t & 1, slot = t % STAGES;
                 if (!wait_or_abort<32>(smem_u32(&sh.full_b[slot]), (t / STAGES) & 1, abort))
                     break;
@@ -317,7 +353,7 @@ __global__ void __launch_bounds__(kThreadsTC, 2) k_search_tc(const uint32_t* __r
 #pragma unroll
                 for (int s = 0; s < KSTEPS; ++s)
                     mma_f8f6f4(tmem + b * kAccCols, smem_desc(a_addr + s * 2 * kChunkBytes, kChunkBytes, 128),
-                           smem_desc(b_addr + s * 2 * kChunkBytes, kChunkBytes, 128), kIdesc,
+                               smem_desc(b_addr + s * 2 * kChunkBytes, kChunkBytes, 128), kIdesc,
                                s > 0 ? 1u : 0u);
                 mma_commit(smem_u32(&sh.acc_full[b]));
                 mma_commit(smem_u32(&sh.b_empty[slot]));
@@ -328,36 +364,64 @@ __global__ void __launch_bounds__(kThreadsTC, 2) k_search_tc(const uint32_t* __r
         }
     } else if (warp >= kEpiWarps) {
         // ---- producers ----
-        // a register ring keeps the descriptors of the next PF tiles in flight
-        constexpr int PF = NW <= 4 ? 4 : 2;
         const int p = tid - 32 * kEpiWarps;
-        auto cand = [&](int t) {
-            return load_desc<NW>(crow + (size_t)min(min(t, ntiles - 1) * kRows + p, cols - 1) * NW);
-        };
-        Desc<NW> ring[PF];
+        if constexpr (PRE) {
 #pragma unroll
-        for (int i = 0; i < PF; ++i)
-            ring[i] = cand(i);
-        expand_desc<NW, ENC>(sA, p, load_desc<NW>(qrow + (size_t)min(m0 + p, cols - 1) * NW),
-                             ENC ? kClearQuery : kClearPlain, kQueryCode);
-        bool live = true;
-        for (int t0 = 0; t0 < ntiles && live; t0 += PF) {
-#pragma unroll
-            for (int i = 0; i < PF; ++i) {
-                const int t = t0 + i;
-                if (t >= ntiles)
-                    break;
-                const Desc<NW> cur = ring[i];
-                ring[i] = cand(t + PF);
-                const int slot = t % STAGES;
-                if (t >= STAGES && !wait_or_abort<64>(smem_u32(&sh.b_empty[slot]), (t / STAGES - 1) & 1, abort)) {
-                    live = false;
-                    break;
+            for (int i = 0; i < kRows / 32; ++i) {
+                const int r = p + 32 * i;
+                expand_desc<NW, ENC>(sA, r, load_desc<NW>(qrow + (size_t)min(m0 + r, cols - 1) * NW),
+                                     ENC ? kClearQuery : kClearPlain, kQueryCode);
+            }
+            fence_async_smem();
+            mbar_arrive(smem_u32(&sh.a_full));
+            if (lane == 0) {
+                const uint8_t* src = (dir ? x0 : x1) + (size_t)row * ntiles * TILE;
+                int issued = -1;
+                for (int t = 0; t < ntiles; ++t) {
+                    const int slot = t % STAGES;
+                    if (t >= STAGES &&
+                        !wait_or_abort<64>(smem_u32(&sh.b_empty[slot]), (t / STAGES - 1) & 1, abort))
+                        break;
+                    mbar_arrive_expect_tx(smem_u32(&sh.full_b[slot]), TILE);
+                    bulk_g2s(smem_u32(sB + slot * TILE), src + (size_t)t * TILE, TILE, smem_u32(&sh.full_b[slot]));
+                    issued = t;
                 }
-                expand_desc<NW, ENC>(sB + slot * TILE, p, cur, ENC ? kClearCand : kClearPlain,
-                                     ENC ? column_code((t & 1) * kRows + p) : 0u);
-                fence_async_smem();
-                mbar_arrive(smem_u32(&sh.full_b[slot]));
+                if (*abort)  // copies still in flight land before the CTA leaves
+                    for (int t = max(0, issued - STAGES + 1); t <= issued; ++t)
+                        wait_drain(smem_u32(&sh.full_b[t % STAGES]), (t / STAGES) & 1);
+            }
+        } else {
+            // a register ring keeps the descriptors of the next PF tiles in flight
+            constexpr int PF = NW <= 4 ? 4 : 2;
+            auto cand = [&](int t) {
+                return load_desc<NW>(crow + (size_t)min(min(t, ntiles - 1) * kRows + p, cols - 1) * NW);
+            };
+            Desc<NW> ring[PF];
+#pragma unroll
+            for (int i = 0; i < PF; ++i)
+                ring[i] = cand(i);
+            expand_desc<NW, ENC>(sA, p, load_desc<NW>(qrow + (size_t)min(m0 + p, cols - 1) * NW),
+                                 ENC ? kClearQuery : kClearPlain, kQueryCode);
+            bool live = true;
+            for (int t0 = 0; t0 < ntiles && live; t0 += PF) {
+#pragma unroll
+                for (int i = 0; i < PF; ++i) {
+                    const int t = t0 + i;
+                    if (t >= ntiles)
+                        break;
+                    const Desc<NW> cur = ring[i];
+                    ring[i] = cand(t + PF);
+                    const int slot = t % STAGES;
+                    if (t >= STAGES &&
+                        !wait_or_abort<64>(smem_u32(&sh.b_empty[slot]), (t / STAGES - 1) & 1, abort)) {
+                        live = false;
+                        break;
+                    }
+                    expand_desc<NW, ENC>(sB + slot * TILE, p, cur, ENC ? kClearCand : kClearPlain,
+                                         ENC ? column_code((t & 1) * kRows + p) : 0u);
+                    fence_async_smem();
+                    mbar_arrive(smem_u32(&sh.full_b[slot]));
+                }
             }
         }
     } else {
@@ -367,6 +431,37 @@ __global__ void __launch_bounds__(kThreadsTC, 2) k_search_tc(const uint32_t* __r
         float mA = -INFINITY, mB = -INFINITY;
         int gA = INT_MIN, gB = INT_MIN;  // column-coded form: global keys
         bool ok = true;
+        // column-coded maxima of one tile's 64 columns (this warp's half):
+        // both 32-column loads in flight before one wait
+        auto coded_max = [&](int u, uint32_t acc) {
+            const int j0 = u * kRows + half * 64, c0 = (u & 1) * kRows + half * 64;
+            if (cols - j0 >= 64) {
+                uint32_t r0[32], r1[32];
+                tmem_ld32_async(acc, r0);
+                tmem_ld32_async(acc + 32, r1);
+                tmem_wait_ld();
+                tmem_hold(r0);
+                tmem_hold(r1);
+                float v[32];
+#pragma unroll
+                for (int j = 0; j < 32; ++j)
+                    v[j] = __uint_as_float(r0[j]);
+                reduce_chunk_coded<NODUP, false>(v, c0, 32, mA, mB);
+#pragma unroll
+                for (int j = 0; j < 32; ++j)
+                    v[j] = __uint_as_float(r1[j]);
+                reduce_chunk_coded<NODUP, false>(v, c0 + 32, 32, mA, mB);
+            } else {
+#pragma unroll
+                for (int ch = 0; ch < 2; ++ch) {
+                    if (j0 + ch * 32 < cols) {
+                        float v[32];
+                        tmem_ld32(acc + ch * 32, v);
+                        reduce_chunk_coded<NODUP, true>(v, c0 + ch * 32, cols - j0 - ch * 32, mA, mB);
+                    }
+                }
+            }
+        };
         for (int t = 0; t < ntiles && ok; ++t) {
             const int b = t & 1;
             ok = wait_or_abort(smem_u32(&sh.acc_full[b]), (t >> 1) & 1, abort);
@@ -374,19 +469,15 @@ __global__ void __launch_bounds__(kThreadsTC, 2) k_search_tc(const uint32_t* __r
             if (!ok)
                 break;
             fence_after();
+            if constexpr (ENC) {
+                coded_max(t, lane_addr + b * kAccCols);
+            } else {
 #pragma unroll
-            for (int ch = 0; ch < 2; ++ch) {
-                const int j0 = t * kRows + half * 64 + ch * 32;
-                if (j0 < cols) {
-                    float v[32];
-                    tmem_ld32(lane_addr + b * kAccCols + ch * 32, v);
-                    if constexpr (ENC) {
-                        const int c0 = (t & 1) * kRows + half * 64 + ch * 32;
-                        if (cols - j0 >= 32)
-                            reduce_chunk_coded<NODUP, false>(v, c0, 32, mA, mB);
-                        else
-                            reduce_chunk_coded<NODUP, true>(v, c0, cols - j0, mA, mB);
-                    } else {
+                for (int ch = 0; ch < 2; ++ch) {
+                    const int j0 = t * kRows + half * 64 + ch * 32;
+                    if (j0 < cols) {
+                        float v[32];
+                        tmem_ld32(lane_addr + b * kAccCols + ch * 32, v);
                         if (cols - j0 >= 32)
                             reduce_chunk<NODUP, false>(v, j0, 32, mA, mB);
                         else
@@ -396,8 +487,11 @@ __global__ void __launch_bounds__(kThreadsTC, 2) k_search_tc(const uint32_t* __r
             }
             fence_before();
             mbar_arrive(smem_u32(&sh.acc_empty[b]));
-            if (ENC && ((t & 1) || t == ntiles - 1))
-                merge_pair<NODUP>(mA, mB, t >> 1, gA, gB);
+            if (ENC && ((t & 1) || t == ntiles - 1)) {
+                decode_a(mA, t >> 1, gA);
+                if constexpr (NODUP)
+                    decode_b(mB, t >> 1, gB);
+            }
         }
         if (half == 1) {
             if constexpr (ENC)
@@ -449,33 +543,61 @@ __global__ void __launch_bounds__(kThreadsTC, 2) k_search_tc(const uint32_t* __r
     }
 }
 
+template<int NW, bool PRE>
+constexpr size_t tc_smem() {
+    // A tile and B ring; at least 80 KB per CTA: at most 2 CTAs (2 x 256
+    // TMEM columns) per SM
+    return (size_t)(1 + b_stages<NW, PRE>()) * kRows * NW * 32 > (size_t)80 * 1024
+               ? (size_t)(1 + b_stages<NW, PRE>()) * kRows * NW * 32
+               : (size_t)80 * 1024;
+}
+
 template<int NW, bool NODUP>
 cudaError_t launch_tc_nw(const uint32_t* d0, const uint32_t* d1, int rows, int cols, int bits, int dirs,
-                         int16_t* disp, long long disp_pitch, int32_t* b0, int32_t* b1, cudaStream_t st) {
+                         int16_t* disp, long long disp_pitch, int32_t* b0, int32_t* b1, uint8_t* xbuf,
+                         cudaStream_t st) {
     constexpr int TILE = kRows * NW * 32;
-    // at least 80 KB per CTA: at most 2 CTAs (2 x 256 TMEM columns) per SM
-    const size_t smem = max((size_t)(1 + b_stages<NW>()) * TILE, (size_t)80 * 1024);
     // column-coded when the two top K slots are padding
-    auto k = bits >= 1 && bits <= 32 * NW - 2 ? k_search_tc<NW, NODUP, true> : k_search_tc<NW, NODUP, false>;
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess)
-        return e;
+    const bool enc = bits >= 1 && bits <= 32 * NW - 2;
     const dim3 grid((cols + kRows - 1) / kRows, rows, dirs);
-    k<<<grid, kThreadsTC, smem, st>>>(d0, d1, rows, cols, disp, disp_pitch, b0, b1);
+    cudaError_t e;
+    if (xbuf && NW <= 8) {
+        // candidate sides expanded once: direction 0 searches d1, direction 1 d0
+        const int ntiles = (cols + kRows - 1) / kRows;
+        const size_t side = (size_t)rows * ntiles * TILE;
+        uint8_t* x1 = xbuf;
+        uint8_t* x0 = dirs > 1 ? xbuf + side : nullptr;
+        const dim3 xg(ntiles, rows);
+        auto xk = enc ? k_expand_tiles<NW, true> : k_expand_tiles<NW, false>;
+        xk<<<xg, kRows, 0, st>>>(d1, cols, ntiles, x1);
+        if (dirs > 1)
+            xk<<<xg, kRows, 0, st>>>(d0, cols, ntiles, x0);
+        auto k = enc ? k_search_tc<NW, NODUP, true, true> : k_search_tc<NW, NODUP, false, true>;
+        constexpr size_t smem = tc_smem<NW, true>();
+        if ((e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
+            return e;
+        k<<<grid, threads_tc<true>(), smem, st>>>(d0, d1, rows, cols, disp, disp_pitch, b0, b1, x0, x1);
+    } else {
+        auto k = enc ? k_search_tc<NW, NODUP, true, false> : k_search_tc<NW, NODUP, false, false>;
+        constexpr size_t smem = tc_smem<NW, false>();
+        if ((e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
+            return e;
+        k<<<grid, threads_tc<false>(), smem, st>>>(d0, d1, rows, cols, disp, disp_pitch, b0, b1, nullptr, nullptr);
+    }
     return cudaGetLastError();
 }
 
 template<bool NODUP>
 cudaError_t launch_tc_dup(const uint32_t* d0, const uint32_t* d1, int rows, int cols, int nwords, int bits,
-                          int dirs, int16_t* disp, long long disp_pitch, int32_t* b0, int32_t* b1,
+                          int dirs, int16_t* disp, long long disp_pitch, int32_t* b0, int32_t* b1, uint8_t* xbuf,
                           cudaStream_t st) {
     switch (nwords) {
-        case 1: return launch_tc_nw<1, NODUP>(d0, d1, rows, cols, bits, dirs, disp, disp_pitch, b0, b1, st);
-        case 2: return launch_tc_nw<2, NODUP>(d0, d1, rows, cols, bits, dirs, disp, disp_pitch, b0, b1, st);
-        case 4: return launch_tc_nw<4, NODUP>(d0, d1, rows, cols, bits, dirs, disp, disp_pitch, b0, b1, st);
-        case 8: return launch_tc_nw<8, NODUP>(d0, d1, rows, cols, bits, dirs, disp, disp_pitch, b0, b1, st);
-        case 12: return launch_tc_nw<12, NODUP>(d0, d1, rows, cols, bits, dirs, disp, disp_pitch, b0, b1, st);
-        case 16: return launch_tc_nw<16, NODUP>(d0, d1, rows, cols, bits, dirs, disp, disp_pitch, b0, b1, st);
+        case 1: return launch_tc_nw<1, NODUP>(d0, d1, rows, cols, bits, dirs, disp, disp_pitch, b0, b1, xbuf, st);
+        case 2: return launch_tc_nw<2, NODUP>(d0, d1, rows, cols, bits, dirs, disp, disp_pitch, b0, b1, xbuf, st);
+        case 4: return launch_tc_nw<4, NODUP>(d0, d1, rows, cols, bits, dirs, disp, disp_pitch, b0, b1, xbuf, st);
+        case 8: return launch_tc_nw<8, NODUP>(d0, d1, rows, cols, bits, dirs, disp, disp_pitch, b0, b1, xbuf, st);
+        case 12: return launch_tc_nw<12, NODUP>(d0, d1, rows, cols, bits, dirs, disp, disp_pitch, b0, b1, xbuf, st);
+        case 16: return launch_tc_nw<16, NODUP>(d0, d1, rows, cols, bits, dirs, disp, disp_pitch, b0, b1, xbuf, st);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -484,15 +606,24 @@ cudaError_t launch_tc_dup(const uint32_t* d0, const uint32_t* d1, int rows, int 
 
 bool search_tc_supported(int cols) { return cols >= 1 && cols <= kMaxCols; }
 
+size_t search_expand_bytes(int rows, int cols, int nwords, int directions) {
+    // wider words take the in-kernel expansion: their tiles leave room for
+    // too few ring slots to hide a bulk copy's latency
+    if (!search_tc_supported(cols) || rows < 1 || nwords > 8)
+        return 0;
+    const size_t ntiles = (size_t)(cols + kRows - 1) / kRows;
+    return (size_t)directions * rows * ntiles * kRows * nwords * 32;
+}
+
 cudaError_t launch_search_tc(const uint32_t* desc0, const uint32_t* desc1, int rows, int cols, int nwords,
                              int bits, bool nodupes, int directions, int16_t* disp, long long disp_pitch,
-                             int32_t* best0, int32_t* best1, cudaStream_t st) {
+                             int32_t* best0, int32_t* best1, cudaStream_t st, uint8_t* xbuf) {
     if (!search_tc_supported(cols) || rows < 1)
         return cudaErrorInvalidValue;
     return nodupes ? launch_tc_dup<true>(desc0, desc1, rows, cols, nwords, bits, directions, disp, disp_pitch,
-                                         best0, best1, st)
+                                         best0, best1, xbuf, st)
                    : launch_tc_dup<false>(desc0, desc1, rows, cols, nwords, bits, directions, disp, disp_pitch,
-                                          best0, best1, st);
+                                          best0, best1, xbuf, st);
 }
 
 unsigned int read_tc_faults() {

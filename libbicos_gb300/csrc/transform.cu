@@ -15,10 +15,41 @@
 namespace bicos_gb300 {
 namespace {
 
+// Bit assembly: each comparison x < y is the sign bit of x - y (the
+// operands are small non-negative integers), shifted into a 32-bit
+// accumulator with one funnel shift, most recent bit lowest; every 32 bits
+// the accumulator, bit-reversed, is one descriptor word (LSB-first).  No
+// predicates and no per-bit masks: a subtraction and a shift per bit.
 template<int NW>
-__device__ __forceinline__ void set_bit(uint32_t (&w)[NW], int pos, bool v) {
-    w[pos >> 5] |= (uint32_t)v << (pos & 31);
-}
+struct BitSink {
+    uint32_t w[NW];
+    uint32_t acc = 0;
+    __device__ __forceinline__ BitSink() {
+#pragma unroll
+        for (int j = 0; j < NW; ++j)
+            w[j] = 0u;
+    }
+    // bit number k (0-based, known at compile time after unrolling) = 1
+    // when d < 0
+    __device__ __forceinline__ void push(int d, int k) {
+        acc = __funnelshift_l((uint32_t)d, acc, 1);
+        if ((k & 31) == 31)
+            w[k >> 5] = __brev(acc);
+    }
+    // the bits pushed since the last full word (count = total pushed, not a
+    // multiple of 32 and possibly known only at run time) into their word
+    __device__ __forceinline__ void flush_partial(int count) {
+        const int r = count & 31;
+        if (r == 0)
+            return;
+        const uint32_t v = __brev(acc) >> (32 - r);
+        const int k = count >> 5;
+#pragma unroll
+        for (int j = 0; j < NW; ++j)
+            if (j == k)
+                w[j] |= v;
+    }
+};
 
 // position known only at run time: select the word without local memory
 template<int NW>
@@ -77,11 +108,7 @@ __device__ __forceinline__ void transform_limited(const StackParams& p, uint32_t
     const float av = __fdiv_rn((float)sum, (float)n);
     const int iav = (int)ceilf(av);  // a < av  <=>  a < ceil(av) for integer a
 
-    uint32_t w[NW];
-#pragma unroll
-    for (int j = 0; j < NW; ++j)
-        w[j] = 0u;
-
+    BitSink<NW> bs;
     int a = v[0], b = v[1];
     int pp = -1, p1 = -1;  // pair sums of steps t-2 and t-1 (reference's prev_pair_sums ring)
 #pragma unroll
@@ -89,12 +116,12 @@ __device__ __forceinline__ void transform_limited(const StackParams& p, uint32_t
         if (t < n - 2) {
             const int c = v[t + 2];
             const int pos = 3 * t + (t >= 2 ? t - 2 : 0);
-            set_bit(w, pos, a < b);
-            set_bit(w, pos + 1, a < c);
-            set_bit(w, pos + 2, a < iav);
+            bs.push(a - b, pos);
+            bs.push(a - c, pos + 1);
+            bs.push(a - iav, pos + 2);
             const int cur = a + b;
             if (t >= 2)
-                set_bit(w, pos + 3, pp < cur);
+                bs.push(pp - cur, pos + 3);
             pp = p1;
             p1 = cur;
             a = b;
@@ -102,12 +129,13 @@ __device__ __forceinline__ void transform_limited(const StackParams& p, uint32_t
         }
     }
     const int pos = 3 * (n - 2) + max(0, n - 4);
-    set_bit_dyn(w, pos, a < b);
-    set_bit_dyn(w, pos + 1, a < iav);
-    set_bit_dyn(w, pos + 2, b < iav);
-    set_bit_dyn(w, pos + 3, pp < a + b);
+    bs.flush_partial(pos);
+    set_bit_dyn(bs.w, pos, a < b);
+    set_bit_dyn(bs.w, pos + 1, a < iav);
+    set_bit_dyn(bs.w, pos + 2, b < iav);
+    set_bit_dyn(bs.w, pos + 3, pp < a + b);
 
-    store_desc(((side ? d1 : d0) + ((size_t)row * p.cols + col) * NW), w);
+    store_desc(((side ? d1 : d0) + ((size_t)row * p.cols + col) * NW), bs.w);
 }
 
 template<typename T, int NW, int NMAX>
@@ -138,35 +166,32 @@ __device__ __forceinline__ void transform_full(const StackParams& p, uint32_t* _
     const float av = __fdiv_rn((float)sum, (float)N);
     const int iav = (int)ceilf(av);
 
-    uint32_t w[NW];
-#pragma unroll
-    for (int j = 0; j < NW; ++j)
-        w[j] = 0u;
-
+    BitSink<NW> bs;
     int ps[N - 1];
     int pos = 0;
 #pragma unroll
     for (int t = 0; t < N - 2; ++t) {
-        set_bit(w, pos++, v[t] < v[t + 1]);
-        set_bit(w, pos++, v[t] < v[t + 2]);
-        set_bit(w, pos++, v[t] < iav);
+        bs.push(v[t] - v[t + 1], pos++);
+        bs.push(v[t] - v[t + 2], pos++);
+        bs.push(v[t] - iav, pos++);
     }
 #pragma unroll
     for (int t = 0; t < N - 1; ++t)
         ps[t] = v[t] + v[t + 1];
-    set_bit(w, pos++, v[N - 2] < v[N - 1]);
-    set_bit(w, pos++, v[N - 2] < iav);
-    set_bit(w, pos++, v[N - 1] < iav);
+    bs.push(v[N - 2] - v[N - 1], pos++);
+    bs.push(v[N - 2] - iav, pos++);
+    bs.push(v[N - 1] - iav, pos++);
 #pragma unroll
     for (int t = 0; t < N - 1; ++t)
 #pragma unroll
         for (int i = 0; i < N - 1; ++i) {
             if (i == t || i == t - 1 || i == t + 1)
                 continue;
-            set_bit(w, pos++, ps[t] < ps[i]);
+            bs.push(ps[t] - ps[i], pos++);
         }
+    bs.flush_partial(pos);
 
-    store_desc(((side ? d1 : d0) + ((size_t)row * p.cols + col) * NW), w);
+    store_desc(((side ? d1 : d0) + ((size_t)row * p.cols + col) * NW), bs.w);
 }
 
 template<typename T, int N>

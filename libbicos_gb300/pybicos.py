@@ -8,10 +8,14 @@ images, and ``invalid_disparity(dtype)``.  Enum values are also exported at
 module level (``pybicos.Full``, ``pybicos.Double`` ...), as
 ``py::enum_::export_values`` does.
 
-``match`` runs on the GPU through ``bicos_match_host_v1``: it uploads the
-images, runs the CUDA path and downloads the results, like the reference's
-CUDA build of pybicos (src/pybicos.cpp:81-95).  ``match_device`` (in
-``libbicos_gb300``) takes CUDA tensors without copies.
+``match`` runs on the GPU.  Given host images (numpy) it goes through
+``bicos_match_host_v1``: upload, the CUDA path, download, like the
+reference's CUDA build of pybicos (src/pybicos.cpp:81-95), and returns
+numpy arrays.  Given device images -- torch CUDA tensors or any object with
+``__cuda_array_interface__`` (CuPy, Numba, ...) -- it matches them where
+they lie, without copies, through ``bicos_match_v1`` and returns torch CUDA
+tensors, enqueued on the producer's stream (torch's current stream, or the
+interface's ``stream``) without a host synchronisation.
 
 One deliberate difference: when ``nxcorr_threshold`` is None the reference
 module fails while converting the never-created correlation map; here
@@ -162,17 +166,103 @@ def _as_image(a) -> np.ndarray:
     return a
 
 
+def _is_device(a) -> bool:
+    return hasattr(a, "__cuda_array_interface__") and not (hasattr(a, "is_cuda") and not a.is_cuda)
+
+
+def _device_image(a):
+    """(bicos_image, stream or None) of a 2-D device array given through
+    __cuda_array_interface__ (version 2 or 3): data pointer, shape,
+    typestr, strides in bytes (None: C-contiguous)."""
+    cai = a.__cuda_array_interface__
+    shape = tuple(cai["shape"])
+    if len(shape) != 2:
+        raise Exception(f"expected 2-D images, got shape {shape}")
+    kinds = {"|u1": (N.BICOS_8U, 1), "<u2": (N.BICOS_16U, 2), "=u2": (N.BICOS_16U, 2)}
+    if cai["typestr"] not in kinds:
+        raise Exception(f"unimplemented cvtype_of(dtype={cai['typestr']})")
+    itype, isz = kinds[cai["typestr"]]
+    rows, cols = shape
+    strides = cai.get("strides") or (cols * isz, isz)
+    if strides[1] != isz or strides[0] < cols * isz:
+        raise Exception("device images need unit column stride and a forward row step of at least one row")
+    ptr = cai["data"][0]
+    return N.image(ptr, rows, cols, itype, strides[0]), cai.get("stream")
+
+
+def _frames_of(stack):
+    """A list of 2-D images, or the 2-D slices of one 3-D (n, rows, cols)
+    device array."""
+    if _is_device(stack) and len(stack.__cuda_array_interface__["shape"]) == 3:
+        return [stack[i] for i in range(stack.__cuda_array_interface__["shape"][0])]
+    return list(stack)
+
+
+def _match_device(stack0, stack1, cfg: Config):
+    """Zero-copy match of device images through bicos_match_v1."""
+    import torch
+
+    from . import _stream_ptr
+    imgs0, imgs1 = [_device_image(a) for a in stack0], [_device_image(a) for a in stack1]
+    first = imgs0[0][0]
+    for im, _ in imgs0 + imgs1:
+        if (im.rows, im.cols, im.type) != (first.rows, first.cols, first.type):
+            raise Exception("all images of both stacks must share size and type")
+    streams = {s for _, s in imgs0 + imgs1 if s not in (None, 1, 2)}
+    if len(streams) > 1:
+        raise Exception("device images from more than one stream")
+    is_torch = hasattr(stack0[0], "device") and hasattr(stack0[0], "data_ptr")
+    dev = stack0[0].device if is_torch else torch.device("cuda", torch.cuda.current_device())
+    stream = C.c_void_p(next(iter(streams))) if streams else _stream_ptr(None)
+    nc = cfg.native()
+    L = N.load()
+    dt, ct = C.c_int32(), C.c_int32()
+    N.check(L.bicos_output_types(C.byref(nc), C.byref(dt), C.byref(ct)))
+    # outputs allocated for the stream the match runs on (torch's caching
+    # allocator ties a block's reuse to its allocation stream)
+    alloc_stream = torch.cuda.ExternalStream(stream.value, device=dev) if streams else torch.cuda.current_stream(dev)
+    with torch.cuda.device(dev), torch.cuda.stream(alloc_stream):
+        disp = torch.empty((first.rows, first.cols), dtype=torch.int16 if dt.value == N.BICOS_16S else torch.float32,
+                           device=dev)
+        corr = None
+        if ct.value >= 0:
+            corr = torch.empty((first.rows, first.cols),
+                               dtype=torch.float64 if ct.value == N.BICOS_64F else torch.float32, device=dev)
+    di = N.tensor_image(disp)
+    ci = N.tensor_image(corr) if corr is not None else None
+    a0 = N.image_array([im for im, _ in imgs0])
+    a1 = N.image_array([im for im, _ in imgs1])
+    st = L.bicos_match_v1(a0, a1, len(imgs0), C.byref(di), C.byref(ci) if ci is not None else None, C.byref(nc),
+                          stream)
+    try:
+        N.check(st)
+    except N.NativeError as e:
+        raise_native(e)
+    return disp, corr
+
+
 def match(stack0, stack1, cfg: Config | None = None):
     """Match two lists of rectified images; returns (disparity, corrmap).
 
     disparity is int16 (INT16_MIN invalid), or float32 (NaN invalid) when a
     subpixel step is set; corrmap is float32 (float64 for Precision.Double),
     NaN where no correlation was computed, or None without a threshold.
+    Host images give numpy results; device images (torch CUDA tensors,
+    __cuda_array_interface__ objects, or one 3-D device stack per side)
+    are matched in place and give torch CUDA tensors.
     """
     if stack0 is None or stack1 is None:
         raise TypeError("stacks must not be None")
     cfg = Config() if cfg is None else cfg
-    stack0, stack1 = list(stack0), list(stack1)
+    stack0, stack1 = _frames_of(stack0), _frames_of(stack1)
+    if stack0 and stack1 and (_is_device(stack0[0]) or _is_device(stack1[0])):
+        if len(stack0) < 2:
+            raise Exception("need at least two images")
+        if len(stack1) != len(stack0):
+            raise Exception("both stacks must hold the same number of images")
+        if not all(_is_device(a) for a in stack0 + stack1):
+            raise Exception("mixing host and device images")
+        return _match_device(stack0, stack1, cfg)
     if not stack0 or not stack1:
         raise Exception("empty stacks")
     if len(stack0) < 2:

@@ -180,16 +180,23 @@ BATCH_SIZES = [(480, 640), (1024, 1280), (1216, 1936), (2048, 2448)]
 BATCH_DEPTHS = [8, 12, 20, 33, 40]
 
 
+# FULL descriptors need n^2 - 2n + 3 bits: n <= 16 within libBICOS's 256,
+# n <= 23 with the 512-bit extension; the deeper stacks of the draw (33, 40:
+# 1026 and 1523 bits) are matched with limited descriptors.
+BATCH_MAX_FULL_N = 23
+
+
 def batch_specs(count: int = 16, seed: int = 0):
     """(rows, cols, n, bits, full, step) per stack, drawn from seed: FULL
-    descriptors only where the reference allows them (n <= 16)."""
+    descriptors where the 512-bit extension allows them (n <= 23; match
+    with max_bits=512), limited otherwise."""
     rng = np.random.default_rng(seed)
     specs = []
     for _ in range(count):
         rows, cols = BATCH_SIZES[int(rng.integers(len(BATCH_SIZES)))]
         n = int(rng.choice(BATCH_DEPTHS))
         bits = 12 if rng.random() < 0.5 else 8
-        full = bool(n <= 16 and rng.random() < 0.5)
+        full = bool(n <= BATCH_MAX_FULL_N and rng.random() < 0.5)
         step = 0.1 if rng.random() < 0.5 else None
         specs.append((rows, cols, n, bits, full, step))
     return specs

@@ -59,11 +59,14 @@ def test_reference_form_rows_vs_oracle(qxga, oracle):
         assert_same(d[r:r + 1], wd, f"row {r}")
         assert_same(corr[r:r + 1], wc, f"row {r} corrmap")
     # whole-frame properties: consistent matches exist, every kept pixel
-    # passed the threshold, disparities stay near the scene's field
+    # passed the threshold, and nearly all of them lie on the scene's
+    # disparity field (without a variance mask a few chance correlations
+    # above 0.9 survive far from it; the planar patches' edges occlude)
     valid = np.isfinite(d)
     assert valid.mean() > 0.5
     assert np.all(corr[valid] >= 0.9)
-    assert np.nanmax(np.abs(d - sc.disparity)) < 150
+    err = np.abs(d[valid] - sc.disparity[valid])
+    assert np.median(err) < 0.5 and np.mean(err < 2.0) > 0.97
 
 
 def test_moment_form_rows_vs_oracle(qxga, oracle):

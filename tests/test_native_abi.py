@@ -108,6 +108,26 @@ def test_errors_before_any_device_work(native):
     assert lib.bicos_match_v1(s, s2, 4, C.byref(d), None, C.byref(c), None) == native.ERR_EXCEPTION
 
 
+def test_points_entry_checks_before_any_device_work(native):
+    """bicos_match_points_v1 validates Q and the points image on the host"""
+    lib = native.load()
+    c = native.default_config()
+    d = native.image(0x10, 4, 8, native.BICOS_16S, 16)
+    s = _stack(native, 4)
+    q = (C.c_double * 16)(*([1.0] * 16))
+    pts = native.image(0x10, 4, 8, native.TYPE_32FC3, 8 * 12)
+    assert lib.bicos_match_points_v1(s, s, 4, C.byref(d), None, C.byref(c), None, C.byref(pts), None) == \
+        native.ERR_INVALID_ARGUMENT
+    small = native.image(0x10, 4, 7, native.TYPE_32FC3, 7 * 12)
+    assert lib.bicos_match_points_v1(s, s, 4, C.byref(d), None, C.byref(c), q, C.byref(small), None) == \
+        native.ERR_EXCEPTION
+    assert b"three-channel float32" in lib.bicos_last_error()
+    q[5] = float("inf")
+    assert lib.bicos_match_points_v1(s, s, 4, C.byref(d), None, C.byref(c), q, C.byref(pts), None) == \
+        native.ERR_INVALID_ARGUMENT
+    assert lib.bicos_last_error() == b"Q must be finite"
+
+
 def test_version(native):
     assert b"sm_103a" in native.load().bicos_version()
 
