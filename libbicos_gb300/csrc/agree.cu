@@ -585,13 +585,16 @@ __device__ __forceinline__ int interp_i(const float4& k, float x) {
 }
 
 // the reference's nxcorrd for sweep point x (left samples, as int bits, in
-// coef[].w)
+// coef[].w); sy: the sum of the point's rounded interpolants when the
+// screening already has it (exact), else -1
 template<typename T, int NMAX>
 __device__ double nxcorrd_at(const float4* coef, int tid, int n, double m0, double var0, float x, bool mv,
-                             double minvar) {
-    long long sy = 0;
-    for (int t = 0; t < n; ++t)
-        sy += interp_i<T>(coef[t * kSubThreads + tid], x);
+                             double minvar, long long sy = -1) {
+    if (sy < 0) {
+        sy = 0;
+        for (int t = 0; t < n; ++t)
+            sy += interp_i<T>(coef[t * kSubThreads + tid], x);
+    }
     const double m1 = __ddiv_rn((double)sy, (double)n);
     double cov = 0.0, var1 = 0.0;
     for (int t = 0; t < n; ++t) {
@@ -704,56 +707,82 @@ __device__ __forceinline__ void subpixel_f64_body(const AgreeParams& p, int bx, 
             float keep_x[kKeep];
             float keep_r[kKeep];
             bool keep_f[kKeep];
+            long long keep_s[kKeep];
             int nk = 0;
             bool overflow = false;
             float best_e = -1.f;  // running best estimate (the sweep starts at -1)
             float xs = -1.f;
+            const f2 one2 = pk(p.one, p.one);
+            constexpr uint32_t kMask = sizeof(T) == 1 ? 0xFFu : 0xFFFFu;
+            // two sweep points per pass on packed FP32 pairs (the same
+            // roundings as interp_i), their moments in exact integers
             while (xs <= 1.f) {
-                Acc s1 = 0, s11 = 0, s01 = 0;
+                float xv[2];
+                bool on[2];
+#pragma unroll
+                for (int g = 0; g < 2; ++g) {
+                    xv[g] = xs;
+                    on[g] = xs <= 1.f;
+                    xs = __fadd_rn(xs, p.step);
+                }
+                const f2 xq = pk(xv[0], xv[1]);
+                Acc s1[2] = {0, 0}, s11[2] = {0, 0}, s01[2] = {0, 0};
                 for (int t = 0; t < n; ++t) {
                     const float4 k = coef[t * kSubThreads + tid];
-                    const Acc v = (Acc)interp_i<T>(k, xs);
-                    s1 += v;
-                    s11 += v * v;
-                    s01 += (Acc)__float_as_int(k.w) * v;
+                    const f2 f = add2(interp2(k.x, k.y, k.z, xq, one2), pk(12582912.0f, 12582912.0f));
+                    uint32_t lo, hi;
+                    asm("mov.b64 {%0, %1}, %2;" : "=r"(lo), "=r"(hi) : "l"(f));
+                    const Acc va = (Acc)(lo & kMask), vb = (Acc)(hi & kMask), xi = (Acc)__float_as_int(k.w);
+                    s1[0] += va;
+                    s11[0] += va * va;
+                    s01[0] += xi * va;
+                    s1[1] += vb;
+                    s11[1] += vb * vb;
+                    s01[1] += xi * vb;
                 }
-                const long long S1 = s1, S11 = s11, S01 = s01;
-                const long long dy = (long long)n * S11 - S1 * S1;
-                const long long num = (long long)n * S01 - sx * S1;
-                bool unsure1 = false;
-                const bool low1 = mv && below(dy, unsure1);
-                unsure1 = mv && unsure1;
-                float re;
-                if (low0 || low1)
-                    re = -1.f;
-                else
-                    re = (float)num * rsqrtf((float)dx * (float)dy);  // NaN when flat
-                const bool forced = unsure0 || unsure1;
-                if (forced || re >= best_e - kWin) {
-                    if (re > best_e) {
-                        // drop kept points that fell out of the window
-                        int w = 0;
-                        for (int i = 0; i < nk; ++i)
-                            if (keep_f[i] || keep_r[i] >= re - kWin) {
-                                keep_x[w] = keep_x[i];
-                                keep_r[w] = keep_r[i];
-                                keep_f[w] = keep_f[i];
-                                ++w;
-                            }
-                        nk = w;
-                        if (!forced)
-                            best_e = re;
-                    }
-                    if (nk < kKeep) {
-                        keep_x[nk] = xs;
-                        keep_r[nk] = re;
-                        keep_f[nk] = forced;
-                        ++nk;
-                    } else {
-                        overflow = true;
+#pragma unroll
+                for (int g = 0; g < 2; ++g) {
+                    if (!on[g])
+                        continue;
+                    const long long S1 = s1[g], S11 = s11[g], S01 = s01[g];
+                    const long long dy = (long long)n * S11 - S1 * S1;
+                    const long long num = (long long)n * S01 - sx * S1;
+                    bool unsure1 = false;
+                    const bool low1 = mv && below(dy, unsure1);
+                    unsure1 = mv && unsure1;
+                    float re;
+                    if (low0 || low1)
+                        re = -1.f;
+                    else
+                        re = (float)num * rsqrtf((float)dx * (float)dy);  // NaN when flat
+                    const bool forced = unsure0 || unsure1;
+                    if (forced || re >= best_e - kWin) {
+                        if (re > best_e) {
+                            // drop kept points that fell out of the window
+                            int w = 0;
+                            for (int i = 0; i < nk; ++i)
+                                if (keep_f[i] || keep_r[i] >= re - kWin) {
+                                    keep_x[w] = keep_x[i];
+                                    keep_r[w] = keep_r[i];
+                                    keep_f[w] = keep_f[i];
+                                    keep_s[w] = keep_s[i];
+                                    ++w;
+                                }
+                            nk = w;
+                            if (!forced)
+                                best_e = re;
+                        }
+                        if (nk < kKeep) {
+                            keep_x[nk] = xv[g];
+                            keep_r[nk] = re;
+                            keep_f[nk] = forced;
+                            keep_s[nk] = S1;
+                            ++nk;
+                        } else {
+                            overflow = true;
+                        }
                     }
                 }
-                xs = __fadd_rn(xs, p.step);
             }
 
             double best = -1.0;
@@ -762,7 +791,7 @@ __device__ __forceinline__ void subpixel_f64_body(const AgreeParams& p, int bx, 
                 for (int i = 0; i < nk; ++i) {
                     if (!keep_f[i] && keep_r[i] < best_e - kWin)
                         continue;
-                    const double r = nxcorrd_at<T, NMAX>(coef, tid, n, m0, var0, keep_x[i], mv, minvar);
+                    const double r = nxcorrd_at<T, NMAX>(coef, tid, n, m0, var0, keep_x[i], mv, minvar, keep_s[i]);
                     if (best < r) {
                         best = r;
                         best_x = keep_x[i];

@@ -139,14 +139,17 @@ __host__ __device__ constexpr int words_for_bits(int bits) {
 // block bodies take the block coordinates as arguments, so the same code
 // runs as a grid over one stack and inside a persistent multi-stack launch
 // (batch.cuh): bx = column block, row, side
-template<typename T, int NW, int NMAX>
+// EXACT: the stack has exactly NMAX frames (the top of its word width's
+// range, e.g. n = 33 for 128-bit words), so every frame loop has a constant
+// trip count and the tail's bit positions are constants too
+template<typename T, int NW, int NMAX, bool EXACT = false>
 __device__ __forceinline__ void transform_limited(const StackParams& p, uint32_t* __restrict__ d0,
                                                   uint32_t* __restrict__ d1, int bx, int row, int side,
                                                   const T* stage = nullptr) {
     const int col = bx * blockDim.x + threadIdx.x;
     if (col >= p.cols)
         return;
-    const int n = p.n;
+    const int n = EXACT ? NMAX : p.n;
 
     int v[NMAX];
     int sum = 0;
@@ -188,7 +191,7 @@ __device__ __forceinline__ void transform_limited(const StackParams& p, uint32_t
     store_desc(((side ? d1 : d0) + ((size_t)row * p.cols + col) * NW), bs.w);
 }
 
-template<typename T, int NW, int NMAX>
+template<typename T, int NW, int NMAX, bool EXACT>
 __global__ void __launch_bounds__(kTfBlock) k_transform_limited(const __grid_constant__ StackParams p,
                                                                 uint32_t* __restrict__ d0,
                                                                 uint32_t* __restrict__ d1, int vec16) {
@@ -196,7 +199,7 @@ __global__ void __launch_bounds__(kTfBlock) k_transform_limited(const __grid_con
     __shared__ uint64_t bar;
     const T* stage = stage_segment<T>(p, blockIdx.z, blockIdx.y, blockIdx.x * kTfBlock, vec16 != 0,
                                       reinterpret_cast<T*>(tf_raw), &bar);
-    transform_limited<T, NW, NMAX>(p, d0, d1, blockIdx.x, blockIdx.y, blockIdx.z, stage);
+    transform_limited<T, NW, NMAX, EXACT>(p, d0, d1, blockIdx.x, blockIdx.y, blockIdx.z, stage);
 }
 
 // full mode: 3 bits per t < n-2, 3 tail bits, then every ordered pair of
@@ -300,12 +303,12 @@ tf_kernel_t<T> pick_full(int n) {
 }
 
 template<typename T>
-tf_kernel_t<T> pick_limited(int nwords) {
+tf_kernel_t<T> pick_limited(int nwords, int n) {
     switch (nwords) {
-        case 1: return k_transform_limited<T, 1, 9>;
-        case 2: return k_transform_limited<T, 2, 17>;
-        case 4: return k_transform_limited<T, 4, 33>;
-        case 8: return k_transform_limited<T, 8, 65>;
+        case 1: return n == 9 ? k_transform_limited<T, 1, 9, true> : k_transform_limited<T, 1, 9, false>;
+        case 2: return n == 17 ? k_transform_limited<T, 2, 17, true> : k_transform_limited<T, 2, 17, false>;
+        case 4: return n == 33 ? k_transform_limited<T, 4, 33, true> : k_transform_limited<T, 4, 33, false>;
+        case 8: return n == 65 ? k_transform_limited<T, 8, 65, true> : k_transform_limited<T, 8, 65, false>;
         default: return nullptr;
     }
 }
@@ -322,7 +325,7 @@ cudaError_t launch_transform(const StackParams& p, int sides, bool full, int nwo
     } else {
         if (words_for_bits(4 * p.n - 7) != nwords)
             return cudaErrorInvalidValue;
-        k = p.elem_bytes == 1 ? pick_limited<uint8_t>(nwords) : pick_limited<uint16_t>(nwords);
+        k = p.elem_bytes == 1 ? pick_limited<uint8_t>(nwords, p.n) : pick_limited<uint16_t>(nwords, p.n);
     }
     if (!k)
         return cudaErrorInvalidValue;
