@@ -13,6 +13,7 @@
 // where the reference leaves its initial fill), so no separate fill pass
 // runs.
 #include <math.h>
+#include <climits>
 
 #include <type_traits>
 
@@ -575,6 +576,17 @@ __global__ void __launch_bounds__(kSubThreads) k_subpixel_f32(const __grid_const
 constexpr int kKeep = 6;
 constexpr float kWin = 1e-5f;
 
+// (double)v for 0 <= v < 2^31, built with integer instructions (exponent
+// from the leading one, the rest of v as the mantissa): exact, and off the
+// FP64 pipe, which this kernel keeps busy with the reference's arithmetic
+__device__ __forceinline__ double exact_double(int v) {
+    const uint32_t u = (uint32_t)v;
+    const int e = 31 - __clz(u | 1u);  // v in [2^e, 2^(e+1)) for v > 0
+    const unsigned long long mant = ((unsigned long long)u << (52 - e)) & 0xFFFFFFFFFFFFFull;
+    const unsigned long long bits = ((unsigned long long)(1023 + e) << 52) | mant;
+    return __longlong_as_double(u ? (long long)bits : 0ll);
+}
+
 // rounded, wrapped interpolant of sweep point x as an integer: the low
 // mantissa bits of q + 1.5*2^23 (see round_wrap_f)
 template<typename T>
@@ -588,8 +600,8 @@ __device__ __forceinline__ int interp_i(const float4& k, float x) {
 // coef[].w); sy: the sum of the point's rounded interpolants when the
 // screening already has it (exact), else -1
 template<typename T, int NMAX>
-__device__ double nxcorrd_at(const float4* coef, int tid, int n, double m0, double var0, float x, bool mv,
-                             double minvar, long long sy = -1) {
+__device__ double nxcorrd_at(const float4* coef, int tid, int n, double m0, double& var0, bool& have_var0, float x,
+                             bool mv, double minvar, long long sy = -1) {
     if (sy < 0) {
         sy = 0;
         for (int t = 0; t < n; ++t)
@@ -597,12 +609,28 @@ __device__ double nxcorrd_at(const float4* coef, int tid, int n, double m0, doub
     }
     const double m1 = __ddiv_rn((double)sy, (double)n);
     double cov = 0.0, var1 = 0.0;
-    for (int t = 0; t < n; ++t) {
-        const float4 k = coef[t * kSubThreads + tid];
-        const double d0 = __dsub_rn((double)__float_as_int(k.w), m0);
-        const double d1 = __dsub_rn((double)interp_i<T>(k, x), m1);
-        cov = __fma_rn(d0, d1, cov);
-        var1 = __fma_rn(d1, d1, var1);
+    if (have_var0) {
+        for (int t = 0; t < n; ++t) {
+            const float4 k = coef[t * kSubThreads + tid];
+            const double d0 = __dsub_rn(exact_double(__float_as_int(k.w)), m0);
+            const double d1 = __dsub_rn(exact_double(interp_i<T>(k, x)), m1);
+            cov = __fma_rn(d0, d1, cov);
+            var1 = __fma_rn(d1, d1, var1);
+        }
+    } else {
+        // the first evaluation of a pixel also accumulates the left
+        // variance (its own chain, in frame order as before)
+        double v0 = 0.0;
+        for (int t = 0; t < n; ++t) {
+            const float4 k = coef[t * kSubThreads + tid];
+            const double d0 = __dsub_rn(exact_double(__float_as_int(k.w)), m0);
+            const double d1 = __dsub_rn(exact_double(interp_i<T>(k, x)), m1);
+            v0 = __fma_rn(d0, d0, v0);
+            cov = __fma_rn(d0, d1, cov);
+            var1 = __fma_rn(d1, d1, var1);
+        }
+        var0 = v0;
+        have_var0 = true;
     }
     if (mv && (var0 < minvar || var1 < minvar))
         return -1.0;
@@ -679,13 +707,12 @@ __device__ __forceinline__ void subpixel_f64_body(const AgreeParams& p, int bx, 
             if (!(corr < (double)p.thr))
                 result = (float)d;
         } else {
-            double var0 = 0.0;
+            double var0 = 0.0;  // accumulated by the first FP64 evaluation
+            bool have_var0 = false;
 #pragma unroll
             for (int t = 0; t < NMAX; ++t) {
                 if (t < n) {
                     const int x = X(t);
-                    const double d0 = __dsub_rn((double)x, m0);
-                    var0 = __fma_rn(d0, d0, var0);
                     const int y0 = YL(t), y1 = YC(t), y2 = YR(t);
                     coef[t * kSubThreads + tid] =
                         make_float4(0.5f * (float)(y0 - 2 * y1 + y2), 0.5f * (float)(y2 - y0), (float)y1,
@@ -695,10 +722,18 @@ __device__ __forceinline__ void subpixel_f64_body(const AgreeParams& p, int bx, 
             // exact left moment and its min-variance decision
             const long long dx = (long long)n * sxx - sx * sx;  // n^2 * variance
             const double mvn = minvar * dn;                    // exact
+            // the min-variance decisions in integers, thresholds made once:
+            // dd < mvn <=> dd < ceil(mvn); the FP64 reference may decide
+            // otherwise only within 1e-9 (relative) of mvn, the band
+            // [ceil(mvn - tol), floor(mvn + tol)]
+            const double tol = 1e-9 * fmax(mvn, 1.0);
+            auto to_ll = [](double v) -> long long {
+                return v >= 9.0e18 ? LLONG_MAX : v <= -9.0e18 ? LLONG_MIN : (long long)v;
+            };
+            const long long cmv = to_ll(ceil(mvn)), ulo = to_ll(ceil(mvn - tol)), uhi = to_ll(floor(mvn + tol));
             auto below = [&](long long dd, bool& unsure) {
-                const double v = (double)dd;  // exact (< 2^53)
-                unsure = fabs(v - mvn) <= 1e-9 * fmax(mvn, 1.0);
-                return v < mvn;
+                unsure = dd >= ulo && dd <= uhi;
+                return dd < cmv;
             };
             bool unsure0;
             const bool low0 = mv && below(dx, unsure0);
@@ -791,7 +826,8 @@ __device__ __forceinline__ void subpixel_f64_body(const AgreeParams& p, int bx, 
                 for (int i = 0; i < nk; ++i) {
                     if (!keep_f[i] && keep_r[i] < best_e - kWin)
                         continue;
-                    const double r = nxcorrd_at<T, NMAX>(coef, tid, n, m0, var0, keep_x[i], mv, minvar, keep_s[i]);
+                    const double r =
+                        nxcorrd_at<T, NMAX>(coef, tid, n, m0, var0, have_var0, keep_x[i], mv, minvar, keep_s[i]);
                     if (best < r) {
                         best = r;
                         best_x = keep_x[i];
@@ -799,7 +835,7 @@ __device__ __forceinline__ void subpixel_f64_body(const AgreeParams& p, int bx, 
                 }
             } else {
                 for (float x = -1.f; x <= 1.f; x = __fadd_rn(x, p.step)) {
-                    const double r = nxcorrd_at<T, NMAX>(coef, tid, n, m0, var0, x, mv, minvar);
+                    const double r = nxcorrd_at<T, NMAX>(coef, tid, n, m0, var0, have_var0, x, mv, minvar);
                     if (best < r) {
                         best = r;
                         best_x = x;

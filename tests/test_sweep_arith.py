@@ -117,3 +117,23 @@ def test_moment_band_exactness_bounds():
     for _ in range(17):
         s = np.float32(s + np.float32(hi16 * hi16))
     assert int(s) != 17 * hi16 * hi16                       # FP32 accumulation rounds there
+
+
+AGREE = open(os.path.join(ROOT, "libbicos_gb300", "csrc", "agree.cu")).read()
+
+
+def test_integer_built_doubles():
+    """exact_double (agree.cu): the FP64 sweep turns samples and rounded
+    interpolants (non-negative, below 2^16) into doubles with integer
+    instructions -- exponent 1023 + e from the leading one at bit e, the
+    value shifted up to the 52-bit mantissa -- instead of a conversion on
+    the FP64 pipe.  Restated here bit for bit over every value below 2^20."""
+    m = re.search(r"double exact_double\(int v\) \{(.*?)\n\}", AGREE, re.S)
+    assert m and "1023 + e" in m.group(1) and "52 - e" in m.group(1) and "0xFFFFFFFFFFFFFull" in m.group(1)
+    v = np.arange(1 << 20, dtype=np.uint64)
+    u = v | np.uint64(1)
+    e = np.floor(np.log2(u.astype(np.float64))).astype(np.uint64)  # exact: u < 2^20
+    mant = (v << (np.uint64(52) - e)) & np.uint64(0xFFFFFFFFFFFFF)
+    bits = ((np.uint64(1023) + e) << np.uint64(52)) | mant
+    bits[v == 0] = 0
+    assert np.array_equal(bits.view(np.float64), v.astype(np.float64))
