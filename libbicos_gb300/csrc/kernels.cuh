@@ -92,7 +92,6 @@ unsigned int read_moment_faults();
 cudaError_t launch_transform(const StackParams& p, int sides, bool full, int nwords,
                              uint32_t* desc0, uint32_t* desc1, cudaStream_t st);
 // number of transform CTAs whose bulk-copy wait ran out (synchronous)
-unsigned int read_tf_faults();
 
 // Row-wise arg-min.  When disp != nullptr (one direction, NODUPES or plain)
 // the kernel writes int16 disparities col0 - best directly; otherwise it

@@ -11,7 +11,6 @@
 // which is the same predicate for integer a.
 #include "batch.cuh"
 #include "kernels.cuh"
-#include "tcgen05.cuh"
 
 namespace bicos_gb300 {
 namespace {
@@ -71,52 +70,6 @@ __device__ __forceinline__ int ld_px(const StackParams& p, int side, int t, int 
 
 constexpr int kTfBlock = 256;  // pixels (threads) per CTA of the grid launches
 
-// Sample t of this thread's pixel: from the CTA's shared copy of the
-// segment (stage != nullptr: frame t at stage + t * kTfBlock) or from
-// global memory.
-template<typename T>
-__device__ __forceinline__ int tf_sample(const StackParams& p, const T* stage, int side, int t, int row, int col) {
-    return stage ? (int)stage[t * kTfBlock + threadIdx.x] : ld_px<T>(p, side, t, row, col);
-}
-
-__device__ unsigned int g_tf_faults = 0;
-
-// The CTA's 256-pixel segment of every frame of one side into shared
-// memory, one bulk copy (cp.async.bulk) per frame completing on an
-// mbarrier: only for whole segments of frames whose rows start 16-byte
-// aligned with 16-byte pitches (vec16), else nullptr and the samples are
-// read per thread.  A wait that runs out (it cannot for valid frames)
-// counts a fault and falls back to the per-thread reads once the copies
-// had time to land.
-template<typename T>
-__device__ __forceinline__ const T* stage_segment(const StackParams& p, int side, int row, int c0, bool vec16,
-                                                  T* stage, uint64_t* bar) {
-    using namespace tc;
-    if (!vec16 || c0 + kTfBlock > p.cols)
-        return nullptr;
-    constexpr uint32_t kSeg = kTfBlock * sizeof(T);
-    const uint32_t b = smem_u32(bar);
-    if (threadIdx.x == 0)
-        mbar_init(b, 1);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        mbar_arrive_expect_tx(b, kSeg * (uint32_t)p.n);
-        for (int t = 0; t < p.n; ++t)
-            bulk_g2s(smem_u32(stage) + t * kSeg,
-                     p.frame[side][t] + (long long)row * p.pitch[side][t] + (long long)c0 * sizeof(T), kSeg, b);
-    }
-    const long long start = clock64();
-    while (!mbar_try_wait(b, 0)) {
-        if (clock64() - start > kWaitCycles) {
-            if (threadIdx.x == 0)
-                atomicAdd(&g_tf_faults, 1u);
-            wait_drain(b, 0);
-            return nullptr;
-        }
-    }
-    return stage;
-}
-
 template<int NW>
 __device__ __forceinline__ void store_desc(uint32_t* out, const uint32_t (&w)[NW]) {
     if constexpr (NW % 4 == 0) {
@@ -144,8 +97,7 @@ __host__ __device__ constexpr int words_for_bits(int bits) {
 // trip count and the tail's bit positions are constants too
 template<typename T, int NW, int NMAX, bool EXACT = false>
 __device__ __forceinline__ void transform_limited(const StackParams& p, uint32_t* __restrict__ d0,
-                                                  uint32_t* __restrict__ d1, int bx, int row, int side,
-                                                  const T* stage = nullptr) {
+                                                  uint32_t* __restrict__ d1, int bx, int row, int side) {
     const int col = bx * blockDim.x + threadIdx.x;
     if (col >= p.cols)
         return;
@@ -155,7 +107,7 @@ __device__ __forceinline__ void transform_limited(const StackParams& p, uint32_t
     int sum = 0;
 #pragma unroll
     for (int t = 0; t < NMAX; ++t) {
-        v[t] = t < n ? tf_sample<T>(p, stage, side, t, row, col) : 0;
+        v[t] = t < n ? ld_px<T>(p, side, t, row, col) : 0;
         sum += v[t];
     }
     const float av = __fdiv_rn((float)sum, (float)n);
@@ -194,12 +146,8 @@ __device__ __forceinline__ void transform_limited(const StackParams& p, uint32_t
 template<typename T, int NW, int NMAX, bool EXACT>
 __global__ void __launch_bounds__(kTfBlock) k_transform_limited(const __grid_constant__ StackParams p,
                                                                 uint32_t* __restrict__ d0,
-                                                                uint32_t* __restrict__ d1, int vec16) {
-    extern __shared__ __align__(16) uint8_t tf_raw[];
-    __shared__ uint64_t bar;
-    const T* stage = stage_segment<T>(p, blockIdx.z, blockIdx.y, blockIdx.x * kTfBlock, vec16 != 0,
-                                      reinterpret_cast<T*>(tf_raw), &bar);
-    transform_limited<T, NW, NMAX, EXACT>(p, d0, d1, blockIdx.x, blockIdx.y, blockIdx.z, stage);
+                                                                uint32_t* __restrict__ d1) {
+    transform_limited<T, NW, NMAX, EXACT>(p, d0, d1, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
 // full mode: 3 bits per t < n-2, 3 tail bits, then every ordered pair of
@@ -207,8 +155,7 @@ __global__ void __launch_bounds__(kTfBlock) k_transform_limited(const __grid_con
 // a constant
 template<typename T, int N>
 __device__ __forceinline__ void transform_full(const StackParams& p, uint32_t* __restrict__ d0,
-                                               uint32_t* __restrict__ d1, int bx, int row, int side,
-                                               const T* stage = nullptr) {
+                                               uint32_t* __restrict__ d1, int bx, int row, int side) {
     constexpr int NW = words_for_bits(N * N - 2 * N + 3);
     const int col = bx * blockDim.x + threadIdx.x;
     if (col >= p.cols)
@@ -218,7 +165,7 @@ __device__ __forceinline__ void transform_full(const StackParams& p, uint32_t* _
     int sum = 0;
 #pragma unroll
     for (int t = 0; t < N; ++t) {
-        v[t] = tf_sample<T>(p, stage, side, t, row, col);
+        v[t] = ld_px<T>(p, side, t, row, col);
         sum += v[t];
     }
     const float av = __fdiv_rn((float)sum, (float)N);
@@ -255,12 +202,8 @@ __device__ __forceinline__ void transform_full(const StackParams& p, uint32_t* _
 template<typename T, int N>
 __global__ void __launch_bounds__(kTfBlock) k_transform_full(const __grid_constant__ StackParams p,
                                                              uint32_t* __restrict__ d0,
-                                                             uint32_t* __restrict__ d1, int vec16) {
-    extern __shared__ __align__(16) uint8_t tf_raw[];
-    __shared__ uint64_t bar;
-    const T* stage = stage_segment<T>(p, blockIdx.z, blockIdx.y, blockIdx.x * kTfBlock, vec16 != 0,
-                                      reinterpret_cast<T*>(tf_raw), &bar);
-    transform_full<T, N>(p, d0, d1, blockIdx.x, blockIdx.y, blockIdx.z, stage);
+                                                             uint32_t* __restrict__ d1) {
+    transform_full<T, N>(p, d0, d1, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
 // persistent multi-stack forms (batch.cuh)
@@ -284,7 +227,7 @@ struct TfFullOp {
 };
 
 template<typename T>
-using tf_kernel_t = void (*)(StackParams, uint32_t*, uint32_t*, int);
+using tf_kernel_t = void (*)(StackParams, uint32_t*, uint32_t*);
 
 template<typename T>
 tf_kernel_t<T> pick_full(int n) {
@@ -317,7 +260,7 @@ tf_kernel_t<T> pick_limited(int nwords, int n) {
 
 cudaError_t launch_transform(const StackParams& p, int sides, bool full, int nwords, uint32_t* desc0,
                              uint32_t* desc1, cudaStream_t st) {
-    void (*k)(StackParams, uint32_t*, uint32_t*, int) = nullptr;
+    void (*k)(StackParams, uint32_t*, uint32_t*) = nullptr;
     if (full) {
         if (words_for_bits(p.n * p.n - 2 * p.n + 3) != nwords)
             return cudaErrorInvalidValue;
@@ -329,23 +272,10 @@ cudaError_t launch_transform(const StackParams& p, int sides, bool full, int nwo
     }
     if (!k)
         return cudaErrorInvalidValue;
-    // bulk-copied segments need every frame row 16-byte aligned
-    bool vec16 = true;
-    for (int side = 0; side < sides && vec16; ++side)
-        for (int t = 0; t < p.n; ++t)
-            if (reinterpret_cast<uintptr_t>(p.frame[side][t]) % 16 != 0 || p.pitch[side][t] % 16 != 0)
-                vec16 = false;
-    const size_t smem = vec16 ? (size_t)p.n * kTfBlock * p.elem_bytes : 0;
     const dim3 block(kTfBlock);
     const dim3 grid((p.cols + kTfBlock - 1) / kTfBlock, p.rows, sides);
-    k<<<grid, block, smem, st>>>(p, desc0, desc1, vec16 ? 1 : 0);
+    k<<<grid, block, 0, st>>>(p, desc0, desc1);
     return cudaGetLastError();
-}
-
-unsigned int read_tf_faults() {
-    unsigned int v = 0;
-    cudaMemcpyFromSymbol(&v, g_tf_faults, sizeof v);
-    return v;
 }
 
 namespace {
