@@ -378,12 +378,20 @@ __device__ __forceinline__ float nxc_from(float cov, float var0, float var1, boo
     return (mv && (var0 < minvar || var1 < minvar)) ? -1.f : __fdiv_rn(cov, __fsqrt_rn(__fmul_rn(var0, var1)));
 }
 
+// Smallest frame count of a bucket: every launcher picks the bucket of a
+// stack with agree_bucket(n), so n is above the previous bucket's maximum
+// and the frame checks below that count fold away at compile time.
+__host__ __device__ constexpr int agree_nmin(int nmax) {
+    return nmax == 8 ? 1 : nmax == 16 ? 9 : nmax == 24 ? 17 : nmax == 33 ? 25 : nmax == 48 ? 34 : 49;
+}
+
 // PREFETCH: request all of a pixel's samples at once (grid launches); the
 // persistent multi-stack form streams them, its claim loop leaving no
 // registers for the prefetch
 template<typename T, int NMAX, bool PREFETCH = true>
 __device__ __forceinline__ void subpixel_f32_body(const AgreeParams& p, int bx, int row) {
     constexpr int XG = NMAX <= 33 ? 4 : 2;
+    constexpr int kNMin = agree_nmin(NMAX);
     // staged per frame and pixel, as planes: (a, b) pairs, c, d0 (each
     // plane [NMAX][kSubThreads]; 16 bytes per frame and pixel in all) --
     // a thread's reads are consecutive across the warp in every plane, so
@@ -416,7 +424,7 @@ __device__ __forceinline__ void subpixel_f32_body(const AgreeParams& p, int bx, 
         if constexpr (kAll) {
 #pragma unroll
             for (int t = 0; t < NMAX; ++t) {
-                if (t < n) {
+                if (t < kNMin || t < n) {
                     xl[t] = sample(0, t, col);
                     yc[t] = sample(1, t, col1);
                     if (!border) {
@@ -434,7 +442,7 @@ __device__ __forceinline__ void subpixel_f32_body(const AgreeParams& p, int bx, 
         if constexpr (kAll) {
 #pragma unroll
             for (int t = 0; t < NMAX; ++t)
-                if (t < n) {
+                if (t < kNMin || t < n) {
                     sx += X(t);
                     sy += YC(t);
                 }
@@ -452,7 +460,7 @@ __device__ __forceinline__ void subpixel_f32_body(const AgreeParams& p, int bx, 
             float cov = 0.f, var0 = 0.f, var1 = 0.f;
 #pragma unroll
             for (int t = 0; t < NMAX; ++t) {
-                if (t < n) {
+                if (t < kNMin || t < n) {
                     const float d0 = __fsub_rn((float)X(t), m0);
                     const float d1 = __fsub_rn((float)YC(t), m1);
                     cov = __fmaf_rn(d0, d1, cov);
@@ -467,7 +475,7 @@ __device__ __forceinline__ void subpixel_f32_body(const AgreeParams& p, int bx, 
             float var0 = 0.f;
 #pragma unroll
             for (int t = 0; t < NMAX; ++t) {
-                if (t < n) {
+                if (t < kNMin || t < n) {
                     const float d0 = __fsub_rn((float)X(t), m0);
                     var0 = __fmaf_rn(d0, d0, var0);
                     const int y0 = YL(t), y1 = YC(t), y2 = YR(t);
@@ -498,7 +506,7 @@ __device__ __forceinline__ void subpixel_f32_body(const AgreeParams& p, int bx, 
                 }
 #pragma unroll
                 for (int t = 0; t < NMAX; ++t) {
-                    if (t < n) {
+                    if (t < kNMin || t < n) {
                         const float2 ab = cab[t * kSubThreads + tid];
                         const float c = cc[t * kSubThreads + tid];
 #pragma unroll
@@ -507,6 +515,11 @@ __device__ __forceinline__ void subpixel_f32_body(const AgreeParams& p, int bx, 
                             s1[q] = add2(s1[q], iv[q][t]);
                         }
                     }
+                    // every fourth frame, a compiler barrier: no coefficient
+                    // load is hoisted across it, which bounds the registers
+                    // the frame-check-free stretch may take
+                    if ((t & 3) == 3)
+                        asm volatile("" ::: "memory");
                 }
                 f2 m1[XP], cov[XP], var1[XP];
 #pragma unroll
@@ -519,7 +532,7 @@ __device__ __forceinline__ void subpixel_f32_body(const AgreeParams& p, int bx, 
                 }
 #pragma unroll
                 for (int t = 0; t < NMAX; ++t) {
-                    if (t < n) {
+                    if (t < kNMin || t < n) {
                         const float d0 = cd0[t * kSubThreads + tid];
                         const f2 D0 = pk(d0, d0);
 #pragma unroll
@@ -529,6 +542,8 @@ __device__ __forceinline__ void subpixel_f32_body(const AgreeParams& p, int bx, 
                             var1[q] = fma2(d1, d1, var1[q]);
                         }
                     }
+                    if ((t & 3) == 3)
+                        asm volatile("" ::: "memory");
                 }
 #pragma unroll
                 for (int g = 0; g < XG; ++g) {
@@ -552,8 +567,10 @@ __device__ __forceinline__ void subpixel_f32_body(const AgreeParams& p, int bx, 
     agree_point(p, row, col, result);
 }
 
+// six CTAs (12 warps) per SM for the 33-frame bucket: the register cap
+// that keeps its sweep within the shared-memory limit's occupancy
 template<typename T, int NMAX>
-__global__ void __launch_bounds__(kSubThreads) k_subpixel_f32(const __grid_constant__ AgreeParams p) {
+__global__ void __launch_bounds__(kSubThreads, NMAX == 33 ? 6 : 1) k_subpixel_f32(const __grid_constant__ AgreeParams p) {
     subpixel_f32_body<T, NMAX>(p, blockIdx.x, blockIdx.y);
 }
 
