@@ -102,12 +102,16 @@ __device__ __forceinline__ void transform_limited(const StackParams& p, uint32_t
     if (col >= p.cols)
         return;
     const int n = EXACT ? NMAX : p.n;
+    // the launchers pick the word width from the bit count 4n - 7, so a
+    // stack of this instance has more frames than the next narrower width
+    // holds and the frame checks below that count fold away
+    constexpr int kNMin = NMAX == 9 ? 2 : NMAX == 17 ? 10 : NMAX == 33 ? 18 : 34;
 
     int v[NMAX];
     int sum = 0;
 #pragma unroll
     for (int t = 0; t < NMAX; ++t) {
-        v[t] = t < n ? ld_px<T>(p, side, t, row, col) : 0;
+        v[t] = (t < kNMin || t < n) ? ld_px<T>(p, side, t, row, col) : 0;
         sum += v[t];
     }
     const float av = __fdiv_rn((float)sum, (float)n);
@@ -118,7 +122,7 @@ __device__ __forceinline__ void transform_limited(const StackParams& p, uint32_t
     int pp = -1, p1 = -1;  // pair sums of steps t-2 and t-1 (reference's prev_pair_sums ring)
 #pragma unroll
     for (int t = 0; t < NMAX - 2; ++t) {
-        if (t < n - 2) {
+        if (t < kNMin - 2 || t < n - 2) {
             const int c = v[t + 2];
             const int pos = 3 * t + (t >= 2 ? t - 2 : 0);
             bs.push(a - b, pos);
