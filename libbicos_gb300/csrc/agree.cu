@@ -738,6 +738,7 @@ __device__ __forceinline__ void subpixel_f64_body(const AgreeParams& p, int bx, 
             }
             // exact left moment and its min-variance decision
             const long long dx = (long long)n * sxx - sx * sx;  // n^2 * variance
+            const Acc dxa = (Acc)dx;
             const double mvn = minvar * dn;                    // exact
             // the min-variance decisions in integers, thresholds made once:
             // dd < mvn <=> dd < ceil(mvn); the FP64 reference may decide
@@ -796,9 +797,12 @@ __device__ __forceinline__ void subpixel_f64_body(const AgreeParams& p, int bx, 
                 for (int g = 0; g < 2; ++g) {
                     if (!on[g])
                         continue;
-                    const long long S1 = s1[g], S11 = s11[g], S01 = s01[g];
-                    const long long dy = (long long)n * S11 - S1 * S1;
-                    const long long num = (long long)n * S01 - sx * S1;
+                    // 8-bit samples: every moment below fits in 32 bits
+                    // (n <= 65: n * sum y^2 < 2^31), so the conversions to
+                    // float are the 32-bit ones
+                    const Acc S1 = s1[g], S11 = s11[g], S01 = s01[g];
+                    const Acc dy = (Acc)n * S11 - S1 * S1;
+                    const Acc num = (Acc)n * S01 - (Acc)sx * S1;
                     bool unsure1 = false;
                     const bool low1 = mv && below(dy, unsure1);
                     unsure1 = mv && unsure1;
@@ -806,7 +810,7 @@ __device__ __forceinline__ void subpixel_f64_body(const AgreeParams& p, int bx, 
                     if (low0 || low1)
                         re = -1.f;
                     else
-                        re = (float)num * rsqrtf((float)dx * (float)dy);  // NaN when flat
+                        re = (float)num * rsqrtf((float)dxa * (float)dy);  // NaN when flat
                     const bool forced = unsure0 || unsure1;
                     if (forced || re >= best_e - kWin) {
                         if (re > best_e) {
