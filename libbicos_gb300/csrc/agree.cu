@@ -661,12 +661,17 @@ __device__ __forceinline__ void subpixel_f64_body(const AgreeParams& p, int bx, 
     const int tid = threadIdx.x;
     const int col = bx * kSubThreads + tid;
     const int cols = p.s.cols, n = p.s.n;
-    if (col >= cols)
-        return;
+    // every lane of the warp stays to the end: pixels whose kept list
+    // overflowed are swept by the whole warp at once
+    const bool live = col < cols;
     float result = NAN;
     double corr = NAN;
-    const int16_t d = reinterpret_cast<const int16_t*>(reinterpret_cast<const char*>(p.raw) + row * p.raw_pitch)[col];
+    const int16_t d = live ? reinterpret_cast<const int16_t*>(reinterpret_cast<const char*>(p.raw) +
+                                                              row * p.raw_pitch)[col]
+                           : kInvalidDisp;
     const int col1 = col - d;
+    bool overflow = false;  // non-border pixel whose kept list overflowed
+    double m0_out = 0.0;
     const bool mv = p.has_minvar != 0;
     const double minvar = (double)p.minvar;
     const double dn = (double)n;
@@ -762,7 +767,6 @@ __device__ __forceinline__ void subpixel_f64_body(const AgreeParams& p, int bx, 
             bool keep_f[kKeep];
             long long keep_s[kKeep];
             int nk = 0;
-            bool overflow = false;
             float best_e = -1.f;  // running best estimate (the sweep starts at -1)
             float xs = -1.f;
             const f2 one2 = pk(p.one, p.one);
@@ -854,20 +858,75 @@ __device__ __forceinline__ void subpixel_f64_body(const AgreeParams& p, int bx, 
                         best_x = keep_x[i];
                     }
                 }
+                corr = best;
+                if (!(best < (double)p.thr))
+                    result = __fsub_rn((float)d, best_x);
             } else {
-                for (float x = -1.f; x <= 1.f; x = __fadd_rn(x, p.step)) {
-                    const double r = nxcorrd_at<T, NMAX>(coef, tid, n, m0, var0, have_var0, x, mv, minvar);
-                    if (best < r) {
-                        best = r;
-                        best_x = x;
-                    }
+                m0_out = m0;  // swept below by the whole warp
+            }
+        }
+    }
+    // Pixels whose kept list overflowed: every sweep point evaluated with
+    // the reference's FP64 arithmetic, one point per lane of the warp, and
+    // the first maximum taken across lanes in sweep order (the sequential
+    // sweep's `best < r` keeps the first of equal maxima, starts from -1
+    // and never takes NaN).  Each lane computes the pixel's left variance
+    // along the way (the same chain, so the same value).
+    unsigned ovf = __ballot_sync(0xffffffffu, overflow);
+    const int lane = tid & 31, wbase = tid & ~31;
+    if (ovf)
+        __syncwarp();  // the swept pixel's staged coefficients, visible to the warp
+    while (ovf) {
+        const int src = __ffs(ovf) - 1;
+        ovf &= ovf - 1;
+        const double m0s = __shfl_sync(0xffffffffu, m0_out, src);
+        double best = -1.0;
+        float best_x = 0.f;
+        float xc = -1.f;  // first sweep point of this chunk of 32
+        bool more = true;
+        while (more) {
+            float x = xc;
+            for (int k = 0; k < lane; ++k)
+                x = __fadd_rn(x, p.step);
+            double r = -INFINITY;
+            if (x <= 1.f) {
+                double v0 = 0.0;
+                bool hv0 = false;
+                r = nxcorrd_at<T, NMAX>(coef, wbase + src, n, m0s, v0, hv0, x, mv, minvar);
+                if (!(r > -1.0))
+                    r = -INFINITY;  // cannot beat the initial -1 (or NaN)
+            }
+            // first maximum across the chunk: larger r, then smaller lane
+            double rb = r;
+            int lb = lane;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const double ro = __shfl_xor_sync(0xffffffffu, rb, o);
+                const int lo = __shfl_xor_sync(0xffffffffu, lb, o);
+                if (ro > rb || (ro == rb && lo < lb)) {
+                    rb = ro;
+                    lb = lo;
                 }
             }
+            const float xb = __shfl_sync(0xffffffffu, x, lb);
+            if (best < rb) {  // chunks in sweep order
+                best = rb;
+                best_x = xb;
+            }
+            // the next chunk starts after the chunk's last point
+            const float xl = __shfl_sync(0xffffffffu, x, 31);
+            xc = __fadd_rn(xl, p.step);
+            more = xl <= 1.f && xc <= 1.f;
+        }
+        if (lane == src) {
             corr = best;
             if (!(best < (double)p.thr))
                 result = __fsub_rn((float)d, best_x);
         }
+        __syncwarp();  // reads of the staged column done before it is reused
     }
+    if (!live)
+        return;
     reinterpret_cast<float*>(reinterpret_cast<char*>(p.out) + row * p.out_pitch)[col] = result;
     put_corr<double>(p, row, col, corr);
     agree_point(p, row, col, result);

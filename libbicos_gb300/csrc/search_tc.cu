@@ -231,8 +231,10 @@ __device__ __forceinline__ void decode_b(float& kB, int pair, int& gB) {
 
 // Warp roles of the pipelined CTA (one CTA = one row x 128 query pixels;
 // the MMA and producer waits back off between polls, the epilogue's do not):
-//   warps 0..7   epilogue: warp w reads TMEM lane quarter w%4, columns
-//                [64*(w/4), 64*(w/4)+64) of each accumulator
+//   warps 0..7   epilogue: warp w reads TMEM lane quarter w%4; column-coded
+//                form: warps 0..3 the even tiles, 4..7 the odd ones, all
+//                128 columns; plain form: columns [64*(w/4), 64*(w/4)+64)
+//                of every tile
 //   producers    in-kernel form (4 warps): thread p expands candidate row p
 //                of each tile into the FP8 ring (and query row p into the
 //                A tile); pre-expanded form (1 warp): the warp expands the
@@ -327,7 +329,9 @@ __global__ void __launch_bounds__(threads_tc<PRE>(), 2) k_search_tc(const uint32
         mbar_init(smem_u32(&sh.a_full), 32 * PROD);
         for (int b = 0; b < 2; ++b) {
             mbar_init(smem_u32(&sh.acc_full[b]), 1);
-            mbar_init(smem_u32(&sh.acc_empty[b]), 32 * kEpiWarps);
+            // column-coded form: one group of four epilogue warps per
+            // accumulator; plain form: all eight warps on every tile
+            mbar_init(smem_u32(&sh.acc_empty[b]), ENC ? 16 * kEpiWarps : 32 * kEpiWarps);
         }
         sh.abort = 0;
     }
@@ -426,15 +430,20 @@ __global__ void __launch_bounds__(threads_tc<PRE>(), 2) k_search_tc(const uint32
         }
     } else {
         // ---- epilogue ----
+        // column-coded form: warps 0..3 take the even tiles, warps 4..7 the
+        // odd ones, each warp all 128 columns of its lane quarter (so the
+        // per-tile waits, loads and decodes are paid once per 128
+        // columns); plain form: warp w reads lane quarter w%4, columns
+        // [64*(w/4), 64*(w/4)+64) of every tile
         const int q = warp & 3, half = warp >> 2;
-        const uint32_t lane_addr = tmem + ((uint32_t)(q * 32) << 16) + half * 64;
+        const uint32_t lane_addr = tmem + ((uint32_t)(q * 32) << 16) + (ENC ? 0 : half * 64);
         float mA = -INFINITY, mB = -INFINITY;
         int gA = INT_MIN, gB = INT_MIN;  // column-coded form: global keys
         bool ok = true;
-        // column-coded maxima of one tile's 64 columns (this warp's half):
-        // both 32-column loads in flight before one wait
-        auto coded_max = [&](int u, uint32_t acc) {
-            const int j0 = u * kRows + half * 64, c0 = (u & 1) * kRows + half * 64;
+        // column-coded maxima of 64 columns [j0, j0 + 64) of tile u: both
+        // 32-column loads in flight before one wait
+        auto coded_max64 = [&](int u, int r, uint32_t acc) {
+            const int j0 = u * kRows + r * 64, c0 = (u & 1) * kRows + r * 64;
             if (cols - j0 >= 64) {
                 uint32_t r0[32], r1[32];
                 tmem_ld32_async(acc, r0);
@@ -462,16 +471,31 @@ __global__ void __launch_bounds__(threads_tc<PRE>(), 2) k_search_tc(const uint32
                 }
             }
         };
-        for (int t = 0; t < ntiles && ok; ++t) {
-            const int b = t & 1;
-            ok = wait_or_abort(smem_u32(&sh.acc_full[b]), (t >> 1) & 1, abort);
-            ok = __all_sync(0xffffffffu, ok);
-            if (!ok)
-                break;
-            fence_after();
-            if constexpr (ENC) {
-                coded_max(t, lane_addr + b * kAccCols);
-            } else {
+        if constexpr (ENC) {
+            for (int t = half; t < ntiles && ok; t += 2) {
+                const int b = t & 1;
+                ok = wait_or_abort(smem_u32(&sh.acc_full[b]), (t >> 1) & 1, abort);
+                ok = __all_sync(0xffffffffu, ok);
+                if (!ok)
+                    break;
+                fence_after();
+                coded_max64(t, 0, lane_addr + b * kAccCols);
+                if (t * kRows + 64 < cols)
+                    coded_max64(t, 1, lane_addr + b * kAccCols + 64);
+                fence_before();
+                mbar_arrive(smem_u32(&sh.acc_empty[b]));
+                decode_a(mA, t >> 1, gA);
+                if constexpr (NODUP)
+                    decode_b(mB, t >> 1, gB);
+            }
+        } else {
+            for (int t = 0; t < ntiles && ok; ++t) {
+                const int b = t & 1;
+                ok = wait_or_abort(smem_u32(&sh.acc_full[b]), (t >> 1) & 1, abort);
+                ok = __all_sync(0xffffffffu, ok);
+                if (!ok)
+                    break;
+                fence_after();
 #pragma unroll
                 for (int ch = 0; ch < 2; ++ch) {
                     const int j0 = t * kRows + half * 64 + ch * 32;
@@ -484,13 +508,8 @@ __global__ void __launch_bounds__(threads_tc<PRE>(), 2) k_search_tc(const uint32
                             reduce_chunk<NODUP, true>(v, j0, cols - j0, mA, mB);
                     }
                 }
-            }
-            fence_before();
-            mbar_arrive(smem_u32(&sh.acc_empty[b]));
-            if (ENC && ((t & 1) || t == ntiles - 1)) {
-                decode_a(mA, t >> 1, gA);
-                if constexpr (NODUP)
-                    decode_b(mB, t >> 1, gB);
+                fence_before();
+                mbar_arrive(smem_u32(&sh.acc_empty[b]));
             }
         }
         if (half == 1) {
