@@ -234,13 +234,14 @@ __device__ __forceinline__ void decode_b(float& kB, int pair, int& gB) {
 //   warps 0..7   epilogue: warp w reads TMEM lane quarter w%4; column-coded
 //                form: warps 0..3 the even tiles, 4..7 the odd ones, all
 //                128 columns; plain form: columns [64*(w/4), 64*(w/4)+64)
-//                of every tile
+//                of every tile; in the pre-expanded form warps 0..3 first
+//                expand the A tile (query row = thread), idle as they are
+//                until the first accumulator is full
 //   producers    in-kernel form (4 warps): thread p expands candidate row p
 //                of each tile into the FP8 ring (and query row p into the
-//                A tile); pre-expanded form (1 warp): the warp expands the
-//                A tile, then one lane moves each candidate tile, already
-//                in FP8 in global memory (k_expand_tiles), into the ring
-//                with one bulk copy
+//                A tile); pre-expanded form (1 warp): one lane moves each
+//                candidate tile, already in FP8 in global memory
+//                (k_expand_tiles), into the ring with one bulk copy
 //   last warp    MMA issue (one lane)
 // A ring of smem B buffers and two TMEM accumulators (2 x 128 columns) let
 // the producers run ahead of the tensor core, which runs one tile ahead of
@@ -265,7 +266,7 @@ __host__ __device__ constexpr int b_stages() {
 struct TcShared {
     uint64_t full_b[kMaxStages];   // producers -> MMA (128 arrivals, or 1 + transaction bytes)
     uint64_t b_empty[kMaxStages];  // MMA commit -> producers (slot read)
-    uint64_t a_full;               // pre-expanded form: A tile written (32 arrivals)
+    uint64_t a_full;               // A tile written (128 arrivals)
     uint64_t acc_full[2];   // MMA commit -> epilogue / producers
     uint64_t acc_empty[2];  // epilogue -> MMA, 256 arrivals
     uint32_t tmem;
@@ -326,7 +327,7 @@ __global__ void __launch_bounds__(threads_tc<PRE>(), 2) k_search_tc(const uint32
             mbar_init(smem_u32(&sh.full_b[s]), PRE ? 1 : 32 * PROD);
             mbar_init(smem_u32(&sh.b_empty[s]), 1);
         }
-        mbar_init(smem_u32(&sh.a_full), 32 * PROD);
+        mbar_init(smem_u32(&sh.a_full), kRows);
         for (int b = 0; b < 2; ++b) {
             mbar_init(smem_u32(&sh.acc_full[b]), 1);
             // column-coded form: one group of four epilogue warps per
@@ -370,14 +371,8 @@ __global__ void __launch_bounds__(threads_tc<PRE>(), 2) k_search_tc(const uint32
         // ---- producers ----
         const int p = tid - 32 * kEpiWarps;
         if constexpr (PRE) {
-#pragma unroll
-            for (int i = 0; i < kRows / 32; ++i) {
-                const int r = p + 32 * i;
-                expand_desc<NW, ENC>(sA, r, load_desc<NW>(qrow + (size_t)min(m0 + r, cols - 1) * NW),
-                                     ENC ? kClearQuery : kClearPlain, kQueryCode);
-            }
-            fence_async_smem();
-            mbar_arrive(smem_u32(&sh.a_full));
+            // the A tile comes from the epilogue warps (idle until the first
+            // accumulator is full); this warp starts the copies at once
             if (lane == 0) {
                 const uint8_t* src = (dir ? x0 : x1) + (size_t)row * ntiles * TILE;
                 int issued = -1;
@@ -430,6 +425,16 @@ __global__ void __launch_bounds__(threads_tc<PRE>(), 2) k_search_tc(const uint32
         }
     } else {
         // ---- epilogue ----
+        if constexpr (PRE) {
+            // pre-expanded form: the first four epilogue warps expand the
+            // A tile (one query row per thread) before the first result
+            if (tid < kRows) {
+                expand_desc<NW, ENC>(sA, tid, load_desc<NW>(qrow + (size_t)min(m0 + tid, cols - 1) * NW),
+                                     ENC ? kClearQuery : kClearPlain, kQueryCode);
+                fence_async_smem();
+                mbar_arrive(smem_u32(&sh.a_full));
+            }
+        }
         // column-coded form: warps 0..3 take the even tiles, warps 4..7 the
         // odd ones, each warp all 128 columns of its lane quarter (so the
         // per-tile waits, loads and decodes are paid once per 128
