@@ -326,3 +326,91 @@ def test_device_views_refuse_host_memory():
         N.points_image(torch.zeros((4, 8, 3), dtype=torch.float32))
     with pytest.raises(ValueError, match="CUDA"):
         lbg.reproject(h16, np.eye(4))
+
+
+# The parts of OpenCV's CUDA core API the adapter uses (cv::cuda::GpuMat's
+# header fields, channels/depth/create, CV_* type codes, Stream::Null and
+# StreamAccessor::getStream), declared as OpenCV 4 declares them.  OpenCV is
+# not installed here; the stand-in lets the adapter's OpenCV branch compile
+# and link against the library in the CPU suite.
+FAKE_CV_CUDA = r"""
+#pragma once
+#include <cstddef>
+#include <cuda_runtime.h>
+#define CV_8U 0
+#define CV_16U 2
+#define CV_16S 3
+#define CV_32F 5
+#define CV_64F 6
+#define CV_16SC1 CV_16S
+#define CV_32FC1 CV_32F
+#define CV_64FC1 CV_64F
+namespace cv { namespace cuda {
+class GpuMat {
+public:
+    int flags = 0, rows = 0, cols = 0;
+    size_t step = 0;
+    unsigned char* data = nullptr;
+    int depth() const { return flags & 7; }
+    int channels() const { return 1; }
+    void create(int r, int c, int type) { rows = r; cols = c; flags = type; }
+};
+class Stream {
+public:
+    static Stream& Null() { static Stream s; return s; }
+    cudaStream_t s_ = nullptr;
+};
+struct StreamAccessor {
+    static cudaStream_t getStream(const Stream& s) { return s.s_; }
+};
+} }
+"""
+
+ADAPTER_CALLER = r"""
+#include <BICOS/opencv.hpp>
+#ifndef EXPECT_OPENCV
+#ifdef BICOS_HAVE_OPENCV_CUDA
+#error "adapter active without OpenCV headers"
+#endif
+int main() { return 0; }
+#else
+#ifndef BICOS_HAVE_OPENCV_CUDA
+#error "adapter not active"
+#endif
+int main() {
+    std::vector<cv::cuda::GpuMat> s0(2), s1(2);
+    cv::cuda::GpuMat disp, corr;
+    BICOS::Config cfg;
+    cfg.subpixel_step = 0.1f;
+    void (*fn)(const std::vector<cv::cuda::GpuMat>&, const std::vector<cv::cuda::GpuMat>&, cv::cuda::GpuMat&,
+               BICOS::Config, cv::cuda::GpuMat*, cv::cuda::Stream&) = &BICOS::match;
+    (void)fn;
+    (void)cfg;
+    return 0;
+}
+#endif
+"""
+
+
+@pytest.mark.parametrize("with_cv", [False, True])
+def test_opencv_adapter_compiles(native, tmp_path, with_cv):
+    """include/BICOS/opencv.hpp (the cv::cuda::GpuMat / cv::cuda::Stream&
+    signature of libBICOS include/match.hpp:30-40) stays out of the way
+    without OpenCV and, given OpenCV's CUDA core headers (a stand-in here),
+    compiles and links against the library."""
+    src = tmp_path / "adapter.cpp"
+    src.write_text(ADAPTER_CALLER)
+    flags = []
+    if with_cv:
+        cv = tmp_path / "cv" / "opencv2" / "core"
+        cv.mkdir(parents=True)
+        (cv / "cuda.hpp").write_text(FAKE_CV_CUDA)
+        (cv / "cuda_stream_accessor.hpp").write_text("#pragma once\n#include <opencv2/core/cuda.hpp>\n")
+        cuda_inc = "/usr/local/cuda/include"
+        if not os.path.isdir(cuda_inc):
+            pytest.skip("CUDA headers not found")
+        flags = ["-DEXPECT_OPENCV", "-I", str(tmp_path / "cv"), "-I", cuda_inc]
+    libdir = os.path.dirname(native.lib_path())
+    subprocess.run(["g++", "-std=c++17", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), *flags, str(src),
+                    "-L", libdir, "-lbicos_gb300", "-Wl,-rpath," + libdir, "-o", str(tmp_path / "adapter")],
+                   check=True)
