@@ -207,8 +207,19 @@ def profile_traffic(kernel):
     return None
 
 
+def sweep_positions(step):
+    """Sweep points per pixel: x = -1, then x += step in float32 (the
+    reference's loop) while x <= 1 -- 20 at step 0.1, whose 21st sum is
+    1.0000001."""
+    x, s, k = np.float32(-1.0), np.float32(step), 0
+    while x <= np.float32(1.0):
+        k += 1
+        x = np.float32(x + s)
+    return k
+
+
 def stage_rooflines(stages, rows, cols, n, clk, valid=0.806, eb=1, nwords=4, dirs=1, full=False,
-                    agree="subpixel_f32", positions=21):
+                    agree="subpixel_f32", positions=None):
     """Roofline of each stage from its live CUDA-event time (ms per launch).
 
     transform: HBM, bytes 2*px*n*eb (stack in) + 2*px*4*nwords (words out)
@@ -222,8 +233,11 @@ def stage_rooflines(stages, rows, cols, n, clk, valid=0.806, eb=1, nwords=4, dir
                peak 152 SMs x 128 lanes x 2 x SM clock) rides along under
                "fp32"
     agree: the agreement kernel ("subpixel_f32", "subpixel_f64", "agree",
-    "moments"); positions: sweep positions per pixel (21 at step 0.1).
+    "moments"); positions: sweep positions per pixel (default: those of
+    the workload's step, 20 at step 0.1).
     """
+    if positions is None:
+        positions = sweep_positions(STEP)
     hbm, bf16, src = peaks()
     px = rows * cols
     sm_mhz = clk.get("sm_mhz") or 2070.0
