@@ -318,15 +318,82 @@ __global__ void __launch_bounds__(kRowsM) k_moments(const __grid_constant__ Mome
                     const bool low0 = mv && V0 < mvn;
                     R best = (R)-1;
                     float best_x = 0.f;
-                    for (float xs = -1.f; xs <= 1.f; xs = __fadd_rn(xs, p.step)) {
-                        const R X = (R)xs;
-                        const R Pv = F::fma(F::fma(P2, X, P1), X, P0);
-                        const R Qv = F::fma(F::fma(F::fma(F::fma(Q4, X, Q3), X, Q2), X, Q1), X, Q0);
-                        const R r = (low0 || (mv && Qv < mvq)) ? (R)-1 : F::ratio(Pv, V0, Qv);
-                        if (best < r) {
-                            best = r;
-                            best_x = xs;
+                    auto eval_all = [&]() {
+                        for (float xs = -1.f; xs <= 1.f; xs = __fadd_rn(xs, p.step)) {
+                            const R X = (R)xs;
+                            const R Pv = F::fma(F::fma(P2, X, P1), X, P0);
+                            const R Qv = F::fma(F::fma(F::fma(F::fma(Q4, X, Q3), X, Q2), X, Q1), X, Q0);
+                            const R r = (low0 || (mv && Qv < mvq)) ? (R)-1 : F::ratio(Pv, V0, Qv);
+                            if (best < r) {
+                                best = r;
+                                best_x = xs;
+                            }
                         }
+                    };
+                    if constexpr (DBL) {
+                        // Every point's P(x) and Q(x) exactly as above, but
+                        // the FP64 ratio (a division and a square root) only
+                        // for points whose single-precision estimate of rho
+                        // (relative error ~1e-6) lies within kMWin of the
+                        // best estimate: every other point is provably below
+                        // the FP64 maximum.  Points the min-variance test
+                        // rejects are -1 and cannot win.  More than kMKeep
+                        // candidates: every point in FP64.
+                        constexpr int kMKeep = 6;
+                        constexpr float kMWin = 1e-5f;
+                        float kx[kMKeep], kr[kMKeep];
+                        R kp[kMKeep], kq[kMKeep];
+                        int nk = 0;
+                        bool overflow = false;
+                        float best_e = -1.f;
+                        const float v0f = (float)V0;
+                        for (float xs = -1.f; xs <= 1.f; xs = __fadd_rn(xs, p.step)) {
+                            const R X = (R)xs;
+                            const R Pv = F::fma(F::fma(P2, X, P1), X, P0);
+                            const R Qv = F::fma(F::fma(F::fma(F::fma(Q4, X, Q3), X, Q2), X, Q1), X, Q0);
+                            if (low0 || (mv && Qv < mvq))
+                                continue;
+                            const float re = (float)Pv * rsqrtf(v0f * (float)Qv);  // NaN kept below
+                            if (re < best_e - kMWin)
+                                continue;
+                            if (re > best_e) {
+                                int w = 0;
+                                for (int i = 0; i < nk; ++i)
+                                    if (!(kr[i] < re - kMWin)) {
+                                        kx[w] = kx[i];
+                                        kr[w] = kr[i];
+                                        kp[w] = kp[i];
+                                        kq[w] = kq[i];
+                                        ++w;
+                                    }
+                                nk = w;
+                                best_e = re;
+                            }
+                            if (nk < kMKeep) {
+                                kx[nk] = xs;
+                                kr[nk] = re;
+                                kp[nk] = Pv;
+                                kq[nk] = Qv;
+                                ++nk;
+                            } else {
+                                overflow = true;
+                            }
+                        }
+                        if (!overflow) {
+                            for (int i = 0; i < nk; ++i) {
+                                if (kr[i] < best_e - kMWin)
+                                    continue;
+                                const R r = F::ratio(kp[i], V0, kq[i]);
+                                if (best < r) {
+                                    best = r;
+                                    best_x = kx[i];
+                                }
+                            }
+                        } else {
+                            eval_all();
+                        }
+                    } else {
+                        eval_all();
                     }
                     corr = best;
                     if (!(best < (R)p.thr))
