@@ -35,6 +35,8 @@
 #include <cuda_fp16.h>
 #include <math.h>
 
+#include <type_traits>
+
 #include "kernels.cuh"
 #include "tcgen05.cuh"
 
@@ -234,32 +236,46 @@ __global__ void __launch_bounds__(kRowsM) k_moments(const __grid_constant__ Mome
         }
     }
 
-    // exact SIMT moments of the left pixel and the right columns
+    // exact SIMT moments of the left pixel and the right columns: 8-bit
+    // samples accumulate in 32 bits (n * 255^2 < 2^31 for n <= 65), 16-bit
+    // ones in 64
+    using Acc = typename std::conditional<sizeof(T) == 1, int, long long>::type;
     long long sx = 0, sxx = 0, sy[kNOff], syy[kNPair];
+    {
+        Acc ax = 0, axx = 0, ay[kNOff], ayy[kNPair];
 #pragma unroll
-    for (int j = 0; j < kNOff; ++j)
-        sy[j] = 0;
+        for (int j = 0; j < kNOff; ++j)
+            ay[j] = 0;
 #pragma unroll
-    for (int j = 0; j < kNPair; ++j)
-        syy[j] = 0;
-    if (valid && ok) {
-        for (int t = 0; t < n; ++t) {
-            const long long x = ld_px<T>(p.s, 0, t, row, col);
-            sx += x;
-            sxx += x * x;
-            long long y[kNOff];
+        for (int j = 0; j < kNPair; ++j)
+            ayy[j] = 0;
+        if (valid && ok) {
+            for (int t = 0; t < n; ++t) {
+                const Acc x = ld_px<T>(p.s, 0, t, row, col);
+                ax += x;
+                axx += x * x;
+                Acc y[kNOff];
 #pragma unroll
-            for (int j = 0; j < kNOff; ++j) {
-                const int c = col1 + j - kR;
-                y[j] = (c >= 0 && c < cols) ? ld_px<T>(p.s, 1, t, row, c) : 0;
-                sy[j] += y[j];
+                for (int j = 0; j < kNOff; ++j) {
+                    const int c = col1 + j - kR;
+                    y[j] = (c >= 0 && c < cols) ? ld_px<T>(p.s, 1, t, row, c) : 0;
+                    ay[j] += y[j];
+                }
+#pragma unroll
+                for (int j = 0; j < kNOff; ++j)
+#pragma unroll
+                    for (int k = j; k < kNOff; ++k)
+                        ayy[pair_index(j, k)] += y[j] * y[k];
             }
-#pragma unroll
-            for (int j = 0; j < kNOff; ++j)
-#pragma unroll
-                for (int k = j; k < kNOff; ++k)
-                    syy[pair_index(j, k)] += y[j] * y[k];
         }
+        sx = ax;
+        sxx = axx;
+#pragma unroll
+        for (int j = 0; j < kNOff; ++j)
+            sy[j] = ay[j];
+#pragma unroll
+        for (int j = 0; j < kNPair; ++j)
+            syy[j] = ayy[j];
     }
 
     const long long nn = n;
@@ -331,59 +347,83 @@ __global__ void __launch_bounds__(kRowsM) k_moments(const __grid_constant__ Mome
                         }
                     };
                     if constexpr (DBL) {
-                        // Every point's P(x) and Q(x) exactly as above, but
-                        // the FP64 ratio (a division and a square root) only
-                        // for points whose single-precision estimate of rho
-                        // (relative error ~1e-6) lies within kMWin of the
-                        // best estimate: every other point is provably below
-                        // the FP64 maximum.  Points the min-variance test
-                        // rejects are -1 and cannot win.  More than kMKeep
+                        // Screening in single precision with a rigorous
+                        // bound, FP64 (the Horner values and the ratio, as
+                        // in eval_all) only for the points that can be the
+                        // FP64 first maximum.  For |x| <= 1 the float Horner
+                        // values Pf, Qf of the float-rounded coefficients
+                        // lie within eP, eQ of the FP64 ones (three and five
+                        // roundings of at most 2^-24 of the coefficients'
+                        // magnitude sum, taken with a margin of 4); rho(x)
+                        // is then bracketed by [lo, hi].  A point is a
+                        // candidate while hi reaches the largest lo seen and
+                        // -1 (which never wins); the min-variance test is
+                        // decided in float when the bound allows, else the
+                        // point is a candidate.  More than kMKeep
                         // candidates: every point in FP64.
                         constexpr int kMKeep = 6;
-                        constexpr float kMWin = 1e-5f;
-                        float kx[kMKeep], kr[kMKeep];
-                        R kp[kMKeep], kq[kMKeep];
+                        float kx[kMKeep], kh[kMKeep];
                         int nk = 0;
                         bool overflow = false;
-                        float best_e = -1.f;
-                        const float v0f = (float)V0;
-                        for (float xs = -1.f; xs <= 1.f; xs = __fadd_rn(xs, p.step)) {
-                            const R X = (R)xs;
-                            const R Pv = F::fma(F::fma(P2, X, P1), X, P0);
-                            const R Qv = F::fma(F::fma(F::fma(F::fma(Q4, X, Q3), X, Q2), X, Q1), X, Q0);
-                            if (low0 || (mv && Qv < mvq))
-                                continue;
-                            const float re = (float)Pv * rsqrtf(v0f * (float)Qv);  // NaN kept below
-                            if (re < best_e - kMWin)
-                                continue;
-                            if (re > best_e) {
-                                int w = 0;
-                                for (int i = 0; i < nk; ++i)
-                                    if (!(kr[i] < re - kMWin)) {
-                                        kx[w] = kx[i];
-                                        kr[w] = kr[i];
-                                        kp[w] = kp[i];
-                                        kq[w] = kq[i];
-                                        ++w;
-                                    }
-                                nk = w;
-                                best_e = re;
-                            }
-                            if (nk < kMKeep) {
-                                kx[nk] = xs;
-                                kr[nk] = re;
-                                kp[nk] = Pv;
-                                kq[nk] = Qv;
-                                ++nk;
-                            } else {
-                                overflow = true;
+                        const float p2 = (float)P2, p1 = (float)P1, p0 = (float)P0;
+                        const float q4 = (float)Q4, q3 = (float)Q3, q2 = (float)Q2, q1 = (float)Q1, q0 = (float)Q0;
+                        const float eP = ldexpf(fabsf(p2) + fabsf(p1) + fabsf(p0), -20);
+                        const float eQ = ldexpf(fabsf(q4) + fabsf(q3) + fabsf(q2) + fabsf(q1) + fabsf(q0), -19);
+                        const float v0f = (float)V0, mvqf = (float)mvq;
+                        const float mv_lo = mvqf * (1.f - 0x1p-20f), mv_hi = mvqf * (1.f + 0x1p-20f);
+                        float best_lo = -1.f;
+                        if (!low0) {
+                            for (float xs = -1.f; xs <= 1.f; xs = __fadd_rn(xs, p.step)) {
+                                const float Pf = __fmaf_rn(__fmaf_rn(p2, xs, p1), xs, p0);
+                                const float Qf =
+                                    __fmaf_rn(__fmaf_rn(__fmaf_rn(__fmaf_rn(q4, xs, q3), xs, q2), xs, q1), xs, q0);
+                                const float qlo = Qf - eQ, qhi = Qf + eQ;
+                                bool unsure = false;
+                                if (mv) {
+                                    if (qhi < mv_lo)
+                                        continue;  // rejected by the min-variance test: -1
+                                    unsure = !(qlo >= mv_hi);
+                                }
+                                float lo = -INFINITY, hi = INFINITY;
+                                if (!unsure && qlo > 0.f) {
+                                    const float plo = Pf - eP, phi = Pf + eP;
+                                    const float s_lo = rsqrtf(v0f * qhi), s_hi = rsqrtf(v0f * qlo);
+                                    hi = phi >= 0.f ? phi * s_hi : phi * s_lo;
+                                    lo = plo >= 0.f ? plo * s_lo : plo * s_hi;
+                                    const float m = ldexpf(fmaxf(fabsf(hi), fabsf(lo)), -20);
+                                    hi += m;
+                                    lo -= m;
+                                }
+                                if (!(hi > -1.f) || hi < best_lo)
+                                    continue;
+                                if (lo > best_lo) {
+                                    best_lo = lo;
+                                    int w = 0;
+                                    for (int i = 0; i < nk; ++i)
+                                        if (!(kh[i] < best_lo)) {
+                                            kx[w] = kx[i];
+                                            kh[w] = kh[i];
+                                            ++w;
+                                        }
+                                    nk = w;
+                                }
+                                if (nk < kMKeep) {
+                                    kx[nk] = xs;
+                                    kh[nk] = hi;
+                                    ++nk;
+                                } else {
+                                    overflow = true;
+                                }
                             }
                         }
                         if (!overflow) {
                             for (int i = 0; i < nk; ++i) {
-                                if (kr[i] < best_e - kMWin)
+                                if (kh[i] < best_lo)
                                     continue;
-                                const R r = F::ratio(kp[i], V0, kq[i]);
+                                const R X = (R)kx[i];
+                                const R Pv = F::fma(F::fma(P2, X, P1), X, P0);
+                                const R Qv = F::fma(F::fma(F::fma(F::fma(Q4, X, Q3), X, Q2), X, Q1), X, Q0);
+                                const R r = (mv && Qv < mvq) ? (R)-1 : F::ratio(Pv, V0, Qv);
                                 if (best < r) {
                                     best = r;
                                     best_x = kx[i];
