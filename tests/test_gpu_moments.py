@@ -42,6 +42,23 @@ def test_moment_form_vs_oracle(cuda, oracle, bits, n, double, step):
     assert_same(host(corr), wc, "corrmap")
 
 
+@pytest.mark.parametrize("bits,n", [(8, 33), (12, 20)])
+@pytest.mark.parametrize("step,mv", [(0.01, 2.0), (0.02, None), (0.1, 400.0), (0.05, 2500.0)])
+def test_moment_form_screening_edges(cuda, oracle, bits, n, step, mv):
+    """the double sweep's single-precision screening (FP64 only for the
+    points its bracket cannot rule out): fine steps (up to 201 points, many
+    near-equal neighbours), no min-variance test, and thresholds close to
+    the pixels' own variances (the test decided in FP64 when the bracket
+    straddles it) -- all bit for bit with the restatement, which evaluates
+    every point in FP64"""
+    sc = scenes.make_scene(24, 240, n, seed=3 * n + bits, bits=bits)
+    raw = raw_disparity(cuda, sc)
+    d, corr = lbg.match_device(dev(sc.left, cuda), dev(sc.right, cuda), cfg(0.5, step, mv, True))
+    wd, wc = oracle.moments(raw, sc.left, sc.right, 0.5, step, None if mv is None else mv * n, True)
+    assert_same(host(d), wd, "disparity")
+    assert_same(host(corr), wc, "corrmap")
+
+
 def test_moment_form_window_fallback(cuda, oracle):
     """tiles whose disparities spread wider than the 64-column window (here:
     planar patches of 5..200 px next to the smooth field, and no threshold on
