@@ -223,6 +223,9 @@ def stage_rooflines(stages, rows, cols, n, clk, valid=0.806, eb=1, nwords=4, dir
     """Roofline of each stage from its live CUDA-event time (ms per launch).
 
     transform: HBM, bytes 2*px*n*eb (stack in) + 2*px*4*nwords (words out)
+               + the FP8 candidate tiles it writes for the tensor-core
+               search (words up to 256 bits, rows up to 4096 columns):
+               dirs*rows*128*ceil(cols/128)*32*nwords
     search:    tensor, 2*rows*cols^2*32*nwords FLOP per direction (+-1 FP8
                dot products over the padded descriptor width) against the
                FP8 dense rate taken as twice the measured bf16 GEMM rate
@@ -243,6 +246,10 @@ def stage_rooflines(stages, rows, cols, n, clk, valid=0.806, eb=1, nwords=4, dir
     sm_mhz = clk.get("sm_mhz") or 2070.0
     t_tf, t_se, t_ag = [max(x, 1e-9) for x in stages]
     tf_bytes = 2 * px * n * eb + 2 * px * 4 * nwords
+    if nwords <= 8 and cols <= 4096:
+        # the transform also writes the searched sides' FP8 candidate tiles
+        # (one byte per descriptor bit slot, whole 128-column tiles)
+        tf_bytes += dirs * rows * ((cols + 127) // 128) * 128 * 32 * nwords
     se_flop = 2.0 * rows * cols * cols * 32 * nwords * dirs
     dbl = agree in ("subpixel_f64", "moments")
     sweep = agree.startswith("subpixel") or agree == "moments"

@@ -326,7 +326,7 @@ cudaError_t build_graph(bicos_batch* b, const std::vector<MatchPlan>& plans, con
                         break;
                     }
                 }
-                r = enqueue_search(plans[i], bufs[i], bs);
+                r = enqueue_search(plans[i], bufs[i], bs, !tf_persistent);
                 if (r != cudaSuccess)
                     *where = "search of item " + std::to_string(i);
             }

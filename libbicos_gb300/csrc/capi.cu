@@ -351,21 +351,32 @@ MatchBuffers bicos_gb300::match_buffers(const MatchPlan& P, void* scratch) {
     return m;
 }
 
+// With an expansion buffer the transform also writes the search's FP8
+// candidate tiles (side 1's for direction 0, then side 0's for direction
+// 1), and enqueue_search finds them there.
 cudaError_t bicos_gb300::enqueue_transform(const MatchPlan& P, const MatchBuffers& m, cudaStream_t st) {
-    return launch_transform(P.s, 2, P.full, P.nw, m.d0, m.d1, st);
+    uint8_t *t0 = nullptr, *t1 = nullptr;
+    if (m.expand) {
+        const size_t ntiles = (size_t)(P.cols + 127) / 128;
+        t1 = m.expand;
+        if (P.consistency)
+            t0 = m.expand + (size_t)P.rows * ntiles * 128 * P.nw * 32;
+    }
+    return launch_transform(P.s, 2, P.full, P.nw, m.d0, m.d1, st, t0, t1, descriptor_positions(P.n, P.full));
 }
 
-cudaError_t bicos_gb300::enqueue_search(const MatchPlan& P, const MatchBuffers& m, cudaStream_t st) {
+cudaError_t bicos_gb300::enqueue_search(const MatchPlan& P, const MatchBuffers& m, cudaStream_t st,
+                                        bool tiles_written) {
     const int bits = descriptor_positions(P.n, P.full);
     if (P.consistency) {
         cudaError_t e = launch_search(m.d0, m.d1, P.rows, P.cols, P.nw, bits, P.cfg->no_dupes != 0, 2, nullptr, 0,
-                                      m.fwd, m.rev, st, m.expand);
+                                      m.fwd, m.rev, st, m.expand, tiles_written && m.expand);
         if (e == cudaSuccess)
             e = launch_consistency(m.fwd, m.rev, P.rows, P.cols, P.cfg->max_lr_diff, m.raw, m.raw_pitch, st);
         return e;
     }
     return launch_search(m.d0, m.d1, P.rows, P.cols, P.nw, bits, true, 1, m.raw, m.raw_pitch, nullptr, nullptr,
-                         st, m.expand);
+                         st, m.expand, tiles_written && m.expand);
 }
 
 AgreeParams bicos_gb300::agree_params(const MatchPlan& P, const MatchBuffers& m) {
@@ -563,7 +574,7 @@ bicos_status run_plan(const MatchPlan& plan, bicos_stream_t stream) {
     if (tev)
         cudaEventRecord(tev[1], st);
     if (e == cudaSuccess)
-        e = enqueue_search(plan, bufs, st);
+        e = enqueue_search(plan, bufs, st, true);
     if (tev)
         cudaEventRecord(tev[2], st);
     if (e == cudaSuccess)

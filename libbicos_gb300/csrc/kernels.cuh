@@ -89,8 +89,13 @@ struct MomentParams {
 cudaError_t launch_moments(const MomentParams& p, int mode, bool dbl, cudaStream_t st);
 unsigned int read_moment_faults();
 
+// tiles0 / tiles1: when set (words up to 256 bits), the transform also
+// writes side 0's / side 1's FP8 candidate tiles for the tensor-core search
+// (the layout k_expand_tiles writes; bits decides the column-coded form),
+// and the search is then told they are there
 cudaError_t launch_transform(const StackParams& p, int sides, bool full, int nwords,
-                             uint32_t* desc0, uint32_t* desc1, cudaStream_t st);
+                             uint32_t* desc0, uint32_t* desc1, cudaStream_t st, uint8_t* tiles0 = nullptr,
+                             uint8_t* tiles1 = nullptr, int bits = 0);
 // number of transform CTAs whose bulk-copy wait ran out (synchronous)
 
 // Row-wise arg-min.  When disp != nullptr (one direction, NODUPES or plain)
@@ -105,8 +110,9 @@ cudaError_t launch_transform(const StackParams& p, int sides, bool full, int nwo
 cudaError_t launch_search(const uint32_t* desc0, const uint32_t* desc1, int rows, int cols,
                           int nwords, int bits, bool nodupes, int directions, int16_t* disp,
                           long long disp_pitch, int32_t* best0, int32_t* best1,
-                          cudaStream_t st, uint8_t* xbuf = nullptr);
-// bytes of the optional expansion scratch (0: the search cannot use one)
+                          cudaStream_t st, uint8_t* xbuf = nullptr, bool xbuf_ready = false);
+// bytes of the optional expansion scratch (0: the search cannot use one);
+// xbuf_ready: the transform already wrote the candidate tiles there
 size_t search_expand_bytes(int rows, int cols, int nwords, int directions);
 
 // point-cloud reprojection (reproject.cu): q = Q row-major, as floats
@@ -125,7 +131,8 @@ cudaError_t launch_reproject(const ReprojectParams& p, bool float_disp, cudaStre
 bool search_tc_supported(int cols);
 cudaError_t launch_search_tc(const uint32_t* desc0, const uint32_t* desc1, int rows, int cols, int nwords,
                              int bits, bool nodupes, int directions, int16_t* disp, long long disp_pitch,
-                             int32_t* best0, int32_t* best1, cudaStream_t st, uint8_t* xbuf = nullptr);
+                             int32_t* best0, int32_t* best1, cudaStream_t st, uint8_t* xbuf = nullptr,
+                             bool xbuf_ready = false);
 // number of tensor-core search CTAs whose bounded waits ran out (synchronous)
 unsigned int read_tc_faults();
 

@@ -50,7 +50,9 @@ bicos_status plan_match(const bicos_image* stack0, const bicos_image* stack1, ui
                         bicos_image* corrmap, const bicos_config* cfg, MatchPlan* plan);
 MatchBuffers match_buffers(const MatchPlan& plan, void* scratch);
 cudaError_t enqueue_transform(const MatchPlan& plan, const MatchBuffers& m, cudaStream_t st);
-cudaError_t enqueue_search(const MatchPlan& plan, const MatchBuffers& m, cudaStream_t st);
+// tiles_written: enqueue_transform wrote the candidate tiles into m.expand
+// (a persistent multi-stack transform does not)
+cudaError_t enqueue_search(const MatchPlan& plan, const MatchBuffers& m, cudaStream_t st, bool tiles_written);
 // parameters of the reference-form agreement (in place on int16 without a
 // step, float output with one)
 AgreeParams agree_params(const MatchPlan& plan, const MatchBuffers& m);

@@ -186,12 +186,12 @@ cudaError_t launch_dup(const uint32_t* d0, const uint32_t* d1, int rows, int col
 
 cudaError_t launch_search(const uint32_t* desc0, const uint32_t* desc1, int rows, int cols, int nwords,
                           int bits, bool nodupes, int directions, int16_t* disp, long long disp_pitch,
-                          int32_t* best0, int32_t* best1, cudaStream_t st, uint8_t* xbuf) {
+                          int32_t* best0, int32_t* best1, cudaStream_t st, uint8_t* xbuf, bool xbuf_ready) {
     if (cols > 32767 || cols < 1 || rows < 1)
         return cudaErrorInvalidValue;
     if (search_tc_supported(cols))
         return launch_search_tc(desc0, desc1, rows, cols, nwords, bits, nodupes, directions, disp, disp_pitch,
-                                best0, best1, st, xbuf);
+                                best0, best1, st, xbuf, xbuf_ready);
     return nodupes ? launch_dup<true>(desc0, desc1, rows, cols, nwords, directions, disp, disp_pitch,
                                       best0, best1, st)
                    : launch_dup<false>(desc0, desc1, rows, cols, nwords, directions, disp, disp_pitch,

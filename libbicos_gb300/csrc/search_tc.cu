@@ -27,6 +27,7 @@
 // and exits.
 #include <climits>
 
+#include "fp8_tiles.cuh"
 #include "kernels.cuh"
 #include "tcgen05.cuh"
 
@@ -37,96 +38,12 @@ __device__ unsigned int g_tc_faults = 0;
 namespace {
 
 using namespace tc;
+using namespace fp8t;
 
-constexpr int kRows = 128;          // MMA M = N = 128
 constexpr float kColScale = 1.0f / 4096.0f;
 constexpr int kMaxCols = 4096;      // key exactness bound
 
-// K-chunk major tiles: the 16 core matrices of one 16-byte K chunk (all 128
-// rows) are contiguous (SBO = 128 B, LBO = 2 KB), so an MMA's operand fetch
-// of one K step walks contiguous shared memory.
-constexpr uint32_t kChunkBytes = 128 * 16;  // one 16-byte K chunk of 128 rows
 constexpr uint32_t kIdesc = tc::idesc_f8_e4m3(kRows, kRows);
-
-// FP8 patterns of a clear bit (a set bit flips bit 7, the sign): +-1, and
-// in the column-coded form +-16 (query rows) and +-8 (candidate rows)
-constexpr uint32_t kClearPlain = 0xB8B8B8B8u;
-constexpr uint32_t kClearQuery = 0xD8D8D8D8u;
-constexpr uint32_t kClearCand = 0xD0D0D0D0u;
-
-// bits 0..3 (lo) or 4..7 (hi) of x -> 4 FP8 bytes: the product puts nibble
-// bit i at bit 8i+7 (the four shifted copies of the nibble do not overlap,
-// so nothing carries), the mask keeps those bits, the XOR applies them to
-// the clear pattern's sign bits
-__device__ __forceinline__ uint32_t fp8_lo(uint32_t x, uint32_t clear4) {
-    return (((x & 0xFu) * 0x10204080u) & 0x80808080u) ^ clear4;
-}
-__device__ __forceinline__ uint32_t fp8_hi(uint32_t x, uint32_t clear4) {
-    return (((x & 0xF0u) * 0x01020408u) & 0x80808080u) ^ clear4;
-}
-
-// e4m3 encoding of the integers 0..15 (exact: at most 4 significant bits)
-__device__ __forceinline__ uint32_t e4m3_small(uint32_t v) {
-    const uint32_t e = 31u - __clz(v | 1u);
-    return v ? ((e + 7u) << 3) | ((v << (3u - e)) & 7u) : 0u;
-}
-
-// byte lanes 2..3 of a row's last 4 K slots: the query row's code factors
-// -1, -16 and a candidate's column nibbles (c < 256)
-constexpr uint32_t kQueryCode = 0xD8B80000u;
-__device__ __forceinline__ uint32_t column_code(uint32_t c) {
-    return (e4m3_small(c & 15u) << 16) | (e4m3_small(c >> 4) << 24);
-}
-
-// one descriptor's words, loaded ahead of its expansion
-template<int NW>
-struct Desc {
-    uint32_t w[NW];
-};
-
-template<int NW>
-__device__ __forceinline__ Desc<NW> load_desc(const uint32_t* p) {
-    Desc<NW> d;
-    if constexpr (NW % 4 == 0) {
-#pragma unroll
-        for (int j = 0; j < NW / 4; ++j) {
-            const uint4 q = __ldg(reinterpret_cast<const uint4*>(p) + j);
-            d.w[4 * j] = q.x;
-            d.w[4 * j + 1] = q.y;
-            d.w[4 * j + 2] = q.z;
-            d.w[4 * j + 3] = q.w;
-        }
-    } else if constexpr (NW == 2) {
-        const uint2 q = __ldg(reinterpret_cast<const uint2*>(p));
-        d.w[0] = q.x;
-        d.w[1] = q.y;
-    } else {
-        d.w[0] = __ldg(p);
-    }
-    return d;
-}
-
-// one descriptor into row rr of a 128-row FP8 tile (canonical layout).
-// code (column-coded form): bytes 2..3 of the row's last 4 K slots,
-// replacing the padding bits there.
-template<int NW, bool ENC>
-__device__ __forceinline__ void expand_desc(uint8_t* tile, int rr, const Desc<NW>& d, uint32_t clear4,
-                                            uint32_t code = 0) {
-    uint8_t* base = tile + (rr >> 3) * 128 + (rr & 7) * 16;
-#pragma unroll
-    for (int w = 0; w < NW; ++w) {
-        const uint32_t x = d.w[w];
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const uint32_t y = x >> (16 * h), z = y >> 8;
-            uint32_t top = fp8_hi(z, clear4);
-            if (ENC && w == NW - 1 && h == 1)
-                top = (top & 0xFFFFu) | code;
-            *reinterpret_cast<uint4*>(base + (2 * w + h) * kChunkBytes) =
-                make_uint4(fp8_lo(y, clear4), fp8_hi(y, clear4), fp8_lo(z, clear4), top);
-        }
-    }
-}
 
 // three-input max (sm_100+): one ALU instruction
 __device__ __forceinline__ float fmax3(float a, float b, float c) {
@@ -579,7 +496,7 @@ constexpr size_t tc_smem() {
 template<int NW, bool NODUP>
 cudaError_t launch_tc_nw(const uint32_t* d0, const uint32_t* d1, int rows, int cols, int bits, int dirs,
                          int16_t* disp, long long disp_pitch, int32_t* b0, int32_t* b1, uint8_t* xbuf,
-                         cudaStream_t st) {
+                         cudaStream_t st, bool ready) {
     constexpr int TILE = kRows * NW * 32;
     // column-coded when the two top K slots are padding
     const bool enc = bits >= 1 && bits <= 32 * NW - 2;
@@ -592,10 +509,12 @@ cudaError_t launch_tc_nw(const uint32_t* d0, const uint32_t* d1, int rows, int c
         uint8_t* x1 = xbuf;
         uint8_t* x0 = dirs > 1 ? xbuf + side : nullptr;
         const dim3 xg(ntiles, rows);
-        auto xk = enc ? k_expand_tiles<NW, true> : k_expand_tiles<NW, false>;
-        xk<<<xg, kRows, 0, st>>>(d1, cols, ntiles, x1);
-        if (dirs > 1)
-            xk<<<xg, kRows, 0, st>>>(d0, cols, ntiles, x0);
+        if (!ready) {
+            auto xk = enc ? k_expand_tiles<NW, true> : k_expand_tiles<NW, false>;
+            xk<<<xg, kRows, 0, st>>>(d1, cols, ntiles, x1);
+            if (dirs > 1)
+                xk<<<xg, kRows, 0, st>>>(d0, cols, ntiles, x0);
+        }
         auto k = enc ? k_search_tc<NW, NODUP, true, true> : k_search_tc<NW, NODUP, false, true>;
         constexpr size_t smem = tc_smem<NW, true>();
         if ((e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
@@ -614,14 +533,26 @@ cudaError_t launch_tc_nw(const uint32_t* d0, const uint32_t* d1, int rows, int c
 template<bool NODUP>
 cudaError_t launch_tc_dup(const uint32_t* d0, const uint32_t* d1, int rows, int cols, int nwords, int bits,
                           int dirs, int16_t* disp, long long disp_pitch, int32_t* b0, int32_t* b1, uint8_t* xbuf,
-                          cudaStream_t st) {
+                          cudaStream_t st, bool ready) {
     switch (nwords) {
-        case 1: return launch_tc_nw<1, NODUP>(d0, d1, rows, cols, bits, dirs, disp, disp_pitch, b0, b1, xbuf, st);
-        case 2: return launch_tc_nw<2, NODUP>(d0, d1, rows, cols, bits, dirs, disp, disp_pitch, b0, b1, xbuf, st);
-        case 4: return launch_tc_nw<4, NODUP>(d0, d1, rows, cols, bits, dirs, disp, disp_pitch, b0, b1, xbuf, st);
-        case 8: return launch_tc_nw<8, NODUP>(d0, d1, rows, cols, bits, dirs, disp, disp_pitch, b0, b1, xbuf, st);
-        case 12: return launch_tc_nw<12, NODUP>(d0, d1, rows, cols, bits, dirs, disp, disp_pitch, b0, b1, xbuf, st);
-        case 16: return launch_tc_nw<16, NODUP>(d0, d1, rows, cols, bits, dirs, disp, disp_pitch, b0, b1, xbuf, st);
+        case 1:
+            return launch_tc_nw<1, NODUP>(d0, d1, rows, cols, bits, dirs, disp, disp_pitch, b0, b1, xbuf, st,
+                                             ready);
+        case 2:
+            return launch_tc_nw<2, NODUP>(d0, d1, rows, cols, bits, dirs, disp, disp_pitch, b0, b1, xbuf, st,
+                                             ready);
+        case 4:
+            return launch_tc_nw<4, NODUP>(d0, d1, rows, cols, bits, dirs, disp, disp_pitch, b0, b1, xbuf, st,
+                                             ready);
+        case 8:
+            return launch_tc_nw<8, NODUP>(d0, d1, rows, cols, bits, dirs, disp, disp_pitch, b0, b1, xbuf, st,
+                                             ready);
+        case 12:
+            return launch_tc_nw<12, NODUP>(d0, d1, rows, cols, bits, dirs, disp, disp_pitch, b0, b1, xbuf, st,
+                                             ready);
+        case 16:
+            return launch_tc_nw<16, NODUP>(d0, d1, rows, cols, bits, dirs, disp, disp_pitch, b0, b1, xbuf, st,
+                                             ready);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -641,13 +572,13 @@ size_t search_expand_bytes(int rows, int cols, int nwords, int directions) {
 
 cudaError_t launch_search_tc(const uint32_t* desc0, const uint32_t* desc1, int rows, int cols, int nwords,
                              int bits, bool nodupes, int directions, int16_t* disp, long long disp_pitch,
-                             int32_t* best0, int32_t* best1, cudaStream_t st, uint8_t* xbuf) {
+                             int32_t* best0, int32_t* best1, cudaStream_t st, uint8_t* xbuf, bool xbuf_ready) {
     if (!search_tc_supported(cols) || rows < 1)
         return cudaErrorInvalidValue;
     return nodupes ? launch_tc_dup<true>(desc0, desc1, rows, cols, nwords, bits, directions, disp, disp_pitch,
-                                         best0, best1, xbuf, st)
+                                         best0, best1, xbuf, st, xbuf_ready)
                    : launch_tc_dup<false>(desc0, desc1, rows, cols, nwords, bits, directions, disp, disp_pitch,
-                                          best0, best1, xbuf, st);
+                                          best0, best1, xbuf, st, xbuf_ready);
 }
 
 unsigned int read_tc_faults() {

@@ -10,6 +10,7 @@
 // sum is exact in int, and `a < mean` is evaluated as `a < ceil(mean)`,
 // which is the same predicate for integer a.
 #include "batch.cuh"
+#include "fp8_tiles.cuh"
 #include "kernels.cuh"
 
 namespace bicos_gb300 {
@@ -84,6 +85,33 @@ __device__ __forceinline__ void store_desc(uint32_t* out, const uint32_t (&w)[NW
     }
 }
 
+// The candidate side's FP8 search tiles, written with the descriptors
+// (fp8_tiles.cuh; what k_expand_tiles makes from them otherwise): x the
+// side's tiles or null, enc the column-coded form.  Columns past the last
+// (up to the tile boundary) repeat the last column's descriptor, as there.
+template<int NW>
+__device__ __forceinline__ void store_tiles(uint8_t* x, int row, int col, int ntiles, int enc,
+                                            const uint32_t (&w)[NW]) {
+    if constexpr (NW <= 8) {
+        fp8t::Desc<NW> d;
+#pragma unroll
+        for (int j = 0; j < NW; ++j)
+            d.w[j] = w[j];
+        if (enc)
+            fp8t::expand_candidate<NW, true>(x, row, col, ntiles, d);
+        else
+            fp8t::expand_candidate<NW, false>(x, row, col, ntiles, d);
+    }
+}
+
+// extra arguments of the grid kernels for the fused tile output
+struct TileOut {
+    uint8_t* x0 = nullptr;  // side 0's tiles (searched in direction 1), or null
+    uint8_t* x1 = nullptr;  // side 1's tiles (searched in direction 0), or null
+    int ntiles = 0;
+    int enc = 0;
+};
+
 __host__ __device__ constexpr int words_for_bits(int bits) {
     return bits <= 32 ? 1 : bits <= 64 ? 2 : bits <= 128 ? 4 : bits <= 256 ? 8 : ((bits + 127) / 128) * 4;
 }
@@ -97,10 +125,14 @@ __host__ __device__ constexpr int words_for_bits(int bits) {
 // trip count and the tail's bit positions are constants too
 template<typename T, int NW, int NMAX, bool EXACT = false>
 __device__ __forceinline__ void transform_limited(const StackParams& p, uint32_t* __restrict__ d0,
-                                                  uint32_t* __restrict__ d1, int bx, int row, int side) {
-    const int col = bx * blockDim.x + threadIdx.x;
-    if (col >= p.cols)
+                                                  uint32_t* __restrict__ d1, int bx, int row, int side,
+                                                  const TileOut& to = TileOut {}) {
+    const int cx = bx * blockDim.x + threadIdx.x;
+    uint8_t* const xt = side ? to.x1 : to.x0;
+    const bool pad = cx >= p.cols;  // a tile row past the last column
+    if (pad && (!xt || cx >= to.ntiles * fp8t::kRows))
         return;
+    const int col = pad ? p.cols - 1 : cx;
     const int n = EXACT ? NMAX : p.n;
     // the launchers pick the word width from the bit count 4n - 7, so a
     // stack of this instance has more frames than the next narrower width
@@ -144,14 +176,17 @@ __device__ __forceinline__ void transform_limited(const StackParams& p, uint32_t
     set_bit_dyn(bs.w, pos + 2, b < iav);
     set_bit_dyn(bs.w, pos + 3, pp < a + b);
 
-    store_desc(((side ? d1 : d0) + ((size_t)row * p.cols + col) * NW), bs.w);
+    if (!pad)
+        store_desc(((side ? d1 : d0) + ((size_t)row * p.cols + col) * NW), bs.w);
+    if (xt)
+        store_tiles<NW>(xt, row, cx, to.ntiles, to.enc, bs.w);
 }
 
 template<typename T, int NW, int NMAX, bool EXACT>
 __global__ void __launch_bounds__(kTfBlock) k_transform_limited(const __grid_constant__ StackParams p,
                                                                 uint32_t* __restrict__ d0,
-                                                                uint32_t* __restrict__ d1) {
-    transform_limited<T, NW, NMAX, EXACT>(p, d0, d1, blockIdx.x, blockIdx.y, blockIdx.z);
+                                                                uint32_t* __restrict__ d1, const TileOut to) {
+    transform_limited<T, NW, NMAX, EXACT>(p, d0, d1, blockIdx.x, blockIdx.y, blockIdx.z, to);
 }
 
 // full mode: 3 bits per t < n-2, 3 tail bits, then every ordered pair of
@@ -159,11 +194,15 @@ __global__ void __launch_bounds__(kTfBlock) k_transform_limited(const __grid_con
 // a constant
 template<typename T, int N>
 __device__ __forceinline__ void transform_full(const StackParams& p, uint32_t* __restrict__ d0,
-                                               uint32_t* __restrict__ d1, int bx, int row, int side) {
+                                               uint32_t* __restrict__ d1, int bx, int row, int side,
+                                               const TileOut& to = TileOut {}) {
     constexpr int NW = words_for_bits(N * N - 2 * N + 3);
-    const int col = bx * blockDim.x + threadIdx.x;
-    if (col >= p.cols)
+    const int cx = bx * blockDim.x + threadIdx.x;
+    uint8_t* const xt = side ? to.x1 : to.x0;
+    const bool pad = cx >= p.cols;  // a tile row past the last column
+    if (pad && (!xt || cx >= to.ntiles * fp8t::kRows))
         return;
+    const int col = pad ? p.cols - 1 : cx;
 
     int v[N];
     int sum = 0;
@@ -200,14 +239,17 @@ __device__ __forceinline__ void transform_full(const StackParams& p, uint32_t* _
         }
     bs.flush_partial(pos);
 
-    store_desc(((side ? d1 : d0) + ((size_t)row * p.cols + col) * NW), bs.w);
+    if (!pad)
+        store_desc(((side ? d1 : d0) + ((size_t)row * p.cols + col) * NW), bs.w);
+    if (xt)
+        store_tiles<NW>(xt, row, cx, to.ntiles, to.enc, bs.w);
 }
 
 template<typename T, int N>
 __global__ void __launch_bounds__(kTfBlock) k_transform_full(const __grid_constant__ StackParams p,
                                                              uint32_t* __restrict__ d0,
-                                                             uint32_t* __restrict__ d1) {
-    transform_full<T, N>(p, d0, d1, blockIdx.x, blockIdx.y, blockIdx.z);
+                                                             uint32_t* __restrict__ d1, const TileOut to) {
+    transform_full<T, N>(p, d0, d1, blockIdx.x, blockIdx.y, blockIdx.z, to);
 }
 
 // persistent multi-stack forms (batch.cuh)
@@ -231,7 +273,7 @@ struct TfFullOp {
 };
 
 template<typename T>
-using tf_kernel_t = void (*)(StackParams, uint32_t*, uint32_t*);
+using tf_kernel_t = void (*)(StackParams, uint32_t*, uint32_t*, TileOut);
 
 template<typename T>
 tf_kernel_t<T> pick_full(int n) {
@@ -263,8 +305,8 @@ tf_kernel_t<T> pick_limited(int nwords, int n) {
 }  // namespace
 
 cudaError_t launch_transform(const StackParams& p, int sides, bool full, int nwords, uint32_t* desc0,
-                             uint32_t* desc1, cudaStream_t st) {
-    void (*k)(StackParams, uint32_t*, uint32_t*) = nullptr;
+                             uint32_t* desc1, cudaStream_t st, uint8_t* tiles0, uint8_t* tiles1, int bits) {
+    void (*k)(StackParams, uint32_t*, uint32_t*, TileOut) = nullptr;
     if (full) {
         if (words_for_bits(p.n * p.n - 2 * p.n + 3) != nwords)
             return cudaErrorInvalidValue;
@@ -276,9 +318,16 @@ cudaError_t launch_transform(const StackParams& p, int sides, bool full, int nwo
     }
     if (!k)
         return cudaErrorInvalidValue;
+    TileOut to;
+    if ((tiles0 || tiles1) && nwords <= 8) {
+        to.x0 = tiles0;
+        to.x1 = sides > 1 ? tiles1 : nullptr;
+        to.ntiles = (p.cols + fp8t::kRows - 1) / fp8t::kRows;
+        to.enc = bits >= 1 && bits <= 32 * nwords - 2;  // the search's column-coded form
+    }
     const dim3 block(kTfBlock);
     const dim3 grid((p.cols + kTfBlock - 1) / kTfBlock, p.rows, sides);
-    k<<<grid, block, 0, st>>>(p, desc0, desc1);
+    k<<<grid, block, 0, st>>>(p, desc0, desc1, to);
     return cudaGetLastError();
 }
 

@@ -1,5 +1,5 @@
 """The tensor-core search's operand encoding and key arithmetic, checked on
-the CPU (csrc/search_tc.cu).
+the CPU (csrc/search_tc.cu, csrc/fp8_tiles.cuh).
 
 The kernel turns each descriptor bit into an FP8 (e4m3) value whose sign is
 the bit, multiplies query and candidate tiles on the tensor cores and reads
@@ -21,7 +21,10 @@ import torch
 
 from conftest import ROOT
 
-SRC = open(os.path.join(ROOT, "libbicos_gb300", "csrc", "search_tc.cu")).read()
+# the byte patterns live in the tile header shared by the search and the
+# transform, the rest in the search
+SRC = "".join(open(os.path.join(ROOT, "libbicos_gb300", "csrc", f)).read()
+              for f in ("fp8_tiles.cuh", "search_tc.cu"))
 CONST = {k: int(v, 16) for k, v in re.findall(r"constexpr uint32_t (k\w+) = (0x[0-9A-Fa-f]+)u;", SRC)}
 M32 = 0xFFFFFFFF
 INV = -32768
