@@ -687,14 +687,15 @@ bicos_status bicos_match_host_v1(const void* const* frames0, const void* const* 
     };
     const long long sp0 = spacing(frames0), sp1 = spacing(frames1);
     const bool dense = host_step == row_bytes;
-    // large stacks: a short first band (its upload is the one that nothing
-    // hides), then three equal bands
-    const int bands = (size_t)rows * cols * n >= ((size_t)32 << 20) && rows >= 64 ? 4 : 1;
+    // large stacks: two short leading bands (5 % and 12 % of the rows: the
+    // first upload is the one that nothing hides, the second has to land
+    // while the first band computes), then three equal bands
+    const int bands = (size_t)rows * cols * n >= ((size_t)32 << 20) && rows >= 64 ? 5 : 1;
     auto band_start = [&](int k) -> int {
         if (bands == 1)
             return k == 0 ? 0 : rows;
-        const int first = rows / 10;
-        return k == 0 ? 0 : first + (int)((long long)(rows - first) * (k - 1) / (bands - 1));
+        const int s1 = rows * 5 / 100, s2 = rows * 17 / 100;
+        return k == 0 ? 0 : k == 1 ? s1 : k == 2 ? s2 : s2 + (int)((long long)(rows - s2) * (k - 2) / 3);
     };
 
     cudaError_t e = cudaEventRecord(hp.fork, st);
