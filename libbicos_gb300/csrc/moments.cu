@@ -250,6 +250,8 @@ __global__ void __launch_bounds__(kRowsM) k_moments(const __grid_constant__ Mome
         for (int j = 0; j < kNPair; ++j)
             ayy[j] = 0;
         if (valid && ok) {
+            // unrolled by four: four frames' samples in flight at once
+#pragma unroll 4
             for (int t = 0; t < n; ++t) {
                 const Acc x = ld_px<T>(p.s, 0, t, row, col);
                 ax += x;
