@@ -21,7 +21,10 @@
 //   -1, -16 in the query row against c's two nibbles in the candidate row)
 // -- the first-arg-max key within a tile pair with no per-candidate
 // arithmetic (integers below 2^17, exact in the FP32 accumulator).  The
-// epilogue decodes each pair's maxima into global keys once per pair.
+// epilogue decodes each tile's maxima into global keys (8192 e -/+ column)
+// once per tile.  The candidate tiles arrive pre-expanded in global memory
+// (written by the transform, or by k_expand_tiles) for words up to 256
+// bits, else producer warps expand them in every CTA.
 // Outputs and semantics are those of k_search (search.cu).  All waits are
 // bounded: a wait that runs out records a fault, and the CTA frees its TMEM
 // and exits.
