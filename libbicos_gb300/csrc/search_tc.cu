@@ -29,6 +29,7 @@
 // bounded: a wait that runs out records a fault, and the CTA frees its TMEM
 // and exits.
 #include <climits>
+#include <type_traits>
 
 #include "fp8_tiles.cuh"
 #include "kernels.cuh"
@@ -396,7 +397,64 @@ __global__ void __launch_bounds__(threads_tc<PRE>(), 2) k_search_tc(const uint32
                 }
             }
         };
-        if constexpr (ENC) {
+        if constexpr (ENC && NODUP) {
+            // column-coded, no-duplicates: one instance per group (tile
+            // parity P), so every candidate's column code c = 128 P + j is a
+            // constant and chain B's D + 2c an addition of an immediate; the
+            // partial maxima run across the whole tile
+            auto run_group = [&](auto par) {
+                constexpr int P = decltype(par)::value;
+                const uint32_t acc = lane_addr + P * kAccCols;
+                for (int t = P; t < ntiles && ok; t += 2) {
+                    ok = wait_or_abort(smem_u32(&sh.acc_full[P]), (t >> 1) & 1, abort);
+                    ok = __all_sync(0xffffffffu, ok);
+                    if (!ok)
+                        break;
+                    fence_after();
+                    if (t * kRows + kRows <= cols) {
+                        float ca[4], cb[4];
+#pragma unroll
+                        for (int i = 0; i < 4; ++i)
+                            ca[i] = cb[i] = -INFINITY;
+#pragma unroll
+                        for (int r = 0; r < 2; ++r) {
+                            uint32_t r0[32], r1[32];
+                            tmem_ld32_async(acc + r * 64, r0);
+                            tmem_ld32_async(acc + r * 64 + 32, r1);
+                            tmem_wait_ld();
+                            tmem_hold(r0);
+                            tmem_hold(r1);
+                            auto chunk = [&](const uint32_t (&rv)[32], int c0) {
+#pragma unroll
+                                for (int k = 0; k < 32; k += 2) {
+                                    const float a = __uint_as_float(rv[k]), bb = __uint_as_float(rv[k + 1]);
+                                    const int c = c0 + k;  // a constant after unrolling
+                                    const int i = (k >> 1) & 3;
+                                    ca[i] = fmax3(ca[i], a, bb);
+                                    cb[i] = fmax3(cb[i], a + (float)(2 * c), bb + (float)(2 * c + 2));
+                                }
+                            };
+                            chunk(r0, P * kRows + r * 64);
+                            chunk(r1, P * kRows + r * 64 + 32);
+                        }
+                        mA = fmax3(mA, fmax3(ca[0], ca[1], ca[2]), ca[3]);
+                        mB = fmax3(mB, fmax3(cb[0], cb[1], cb[2]), cb[3]);
+                    } else {
+                        coded_max64(t, 0, acc);
+                        if (t * kRows + 64 < cols)
+                            coded_max64(t, 1, acc + 64);
+                    }
+                    fence_before();
+                    mbar_arrive(smem_u32(&sh.acc_empty[P]));
+                    decode_a(mA, t >> 1, gA);
+                    decode_b(mB, t >> 1, gB);
+                }
+            };
+            if (half == 0)
+                run_group(std::integral_constant<int, 0> {});
+            else
+                run_group(std::integral_constant<int, 1> {});
+        } else if constexpr (ENC) {
             for (int t = half; t < ntiles && ok; t += 2) {
                 const int b = t & 1;
                 ok = wait_or_abort(smem_u32(&sh.acc_full[b]), (t >> 1) & 1, abort);
