@@ -110,9 +110,9 @@ typedef struct bicos_config {
  * correlation is a closed-form function of the position; FP64 (precision
  * double) or FP32 evaluates only the final polynomials and ratio.  Results
  * differ from the reference's by the rounding of its interpolants.  The
- * moments are exact for 8-bit samples and for 16-bit samples below 4096
- * (12-bit data); with wider 16-bit samples the tensor-core band sums can
- * pass 2^24 and round in FP32 (relative error of order n * 2^-24). */
+ * moments are exact integers for every input: 8-bit samples and 16-bit
+ * samples below 4096 take the tensor-core band, tiles holding a larger
+ * 16-bit sample the SIMT sums. */
 enum { BICOS_NXCORR_REFERENCE = 0, BICOS_NXCORR_MOMENTS = 1, BICOS_NXCORR_LEARNED = 2 };
 /* LEARNED (extension, no counterpart in the reference; subpixel runs only,
  * other runs take the reference form): a small network proposes each

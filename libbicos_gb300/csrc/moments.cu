@@ -14,9 +14,9 @@
 // FP32 results are exact for 8-bit stacks (n <= 65).  12-bit data is split
 // into 6-bit halves, x = 64 xh + xl: Sxy = 4096 (xh.yh) + 64 (xh.yl +
 // xl.yh) + xl.yl from three accumulators, exact for samples below 4096;
-// wider 16-bit samples give xh up to 1023, and the xh.yh sums can pass 2^24
-// and round.  Tiles whose disparities spread wider than the window use SIMT
-// dot products (the same integers).
+// wider 16-bit samples give xh up to 1023, whose sums can pass 2^24, so a
+// tile that stages such a sample uses SIMT dot products (the same
+// integers), as do tiles whose disparities spread wider than the window.
 //
 // Leaving the sweep's quadratic interpolant unrounded, I(x) = a x^2 + b x + c
 // (a, b, c from y at col1-1, col1, col1+1), the sweep correlation is
@@ -91,6 +91,7 @@ struct MomShared {
     uint32_t tmem;
     int abort;
     int cmin, cmax;
+    int big;  // 16-bit stacks: a staged sample of 4096 or more
 };
 
 template<bool DBL>
@@ -147,6 +148,7 @@ __global__ void __launch_bounds__(kRowsM) k_moments(const __grid_constant__ Mome
         sh.abort = 0;
         sh.cmin = 0x7fffffff;
         sh.cmax = -0x7fffffff;
+        sh.big = 0;
     }
     fence_before();
     __syncthreads();
@@ -157,7 +159,25 @@ __global__ void __launch_bounds__(kRowsM) k_moments(const __grid_constant__ Mome
     }
     __syncthreads();
     const int wlo = sh.cmin - kR;
-    const bool use_tc = sh.cmax >= sh.cmin && sh.cmax + kR - wlo < kWin;
+    bool use_tc = sh.cmax >= sh.cmin && sh.cmax + kR - wlo < kWin;
+    if constexpr (sizeof(T) == 2) {
+        // the 6+6-bit split is exact only for samples below 4096 (the high
+        // parts' products summed over the frames stay below 2^24); a tile
+        // that stages a larger one takes the exact SIMT sums instead
+        if (use_tc) {
+            bool big = false;
+            for (int t = 0; t < n; ++t) {
+                if (valid)
+                    big |= ld_px<T>(p.s, 0, t, row, col) >= 4096;
+                if (tid < kWin && wlo + tid >= 0 && wlo + tid < cols)
+                    big |= ld_px<T>(p.s, 1, t, row, wlo + tid) >= 4096;
+            }
+            if (big)
+                atomicOr(&sh.big, 1);
+        }
+        __syncthreads();
+        use_tc = use_tc && !sh.big;
+    }
 
     long long sxy[kNOff];
 #pragma unroll

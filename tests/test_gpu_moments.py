@@ -59,6 +59,24 @@ def test_moment_form_screening_edges(cuda, oracle, bits, n, step, mv):
     assert_same(host(corr), wc, "corrmap")
 
 
+@pytest.mark.parametrize("step", [None, 0.1])
+def test_moment_form_full_16bit(cuda, oracle, step):
+    """16-bit samples over the full range (up to 65535, beyond the 6+6-bit
+    split's exact range): tiles holding a sample of 4096 or more take the
+    exact SIMT sums, so the moments stay exact integers and the results
+    equal the restatement bit for bit"""
+    sc = scenes.make_scene(24, 256, 20, seed=11, bits=12)
+    left = (sc.left.astype(np.uint32) * 16 + 7).clip(0, 65535).astype(np.uint16)
+    right = (sc.right.astype(np.uint32) * 16 + 7).clip(0, 65535).astype(np.uint16)
+    assert left.max() >= 4096
+    raw, _ = lbg.match_device(dev(left, cuda), dev(right, cuda), cfg(thr=None))
+    raw = host(raw)
+    d, corr = lbg.match_device(dev(left, cuda), dev(right, cuda), cfg(0.5, step, 2.0, True))
+    wd, wc = oracle.moments(raw, left, right, 0.5, step, 2.0 * 20, True)
+    assert_same(host(d), wd, "disparity")
+    assert_same(host(corr), wc, "corrmap")
+
+
 def test_moment_form_window_fallback(cuda, oracle):
     """tiles whose disparities spread wider than the 64-column window (here:
     planar patches of 5..200 px next to the smooth field, and no threshold on

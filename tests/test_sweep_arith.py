@@ -99,7 +99,9 @@ def test_small_int_to_float_exhaustive():
 def test_moment_band_exactness_bounds():
     """The moment form's tensor-core band (csrc/moments.cu): FP16 operands,
     FP32 sums.  Every operand must be an FP16 integer (below 2048) and every
-    partial sum below 2^24 for the band to be exact."""
+    partial sum below 2^24 for the band to be exact -- which holds for 8-bit
+    samples and for 16-bit samples below 4096, the range the kernel sends
+    to the tensor cores."""
     n_max = 65
     assert 255 * 255 * n_max < 2 ** 24                      # 8-bit samples
     hi, lo = 4095 >> 6, 4095 & 63                           # 12-bit: 6 + 6 bits
@@ -110,7 +112,9 @@ def test_moment_band_exactness_bounds():
     x = np.arange(4096, dtype=np.int64)
     assert np.array_equal(4096 * ((x >> 6) * (x >> 6)) + 64 * (2 * (x >> 6) * (x & 63)) + (x & 63) ** 2, x * x)
     # past 12 bits the high part reaches 1023 and its sums pass 2^24 from
-    # n = 17 on: the documented limit of the form
+    # n = 17 on: a tile that stages a sample of 4096 or more takes the exact
+    # SIMT sums instead (moments.cu; checked on the GPU in
+    # tests/test_gpu_moments.py::test_moment_form_full_16bit)
     hi16 = 65535 >> 6
     assert hi16 < 2048 and hi16 * hi16 * 16 < 2 ** 24 <= hi16 * hi16 * 17
     s = np.float32(0)
