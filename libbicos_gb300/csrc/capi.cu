@@ -422,15 +422,17 @@ cudaError_t bicos_gb300::enqueue_agree(const MatchPlan& P, const MatchBuffers& m
     if (!P.thr)
         return P.pts ? reproject_after(P, st) : cudaSuccess;
     AgreeParams ap = agree_params(P, m);
-    if (P.pts && !P.moments && !P.learned) {  // fused: the agreement kernel writes the points
+    // the reference and moment forms' kernels write the points themselves;
+    // the learned form's sweep list rewrites pixels after its first kernel
+    const bool fused = P.pts && !P.learned;
+    if (fused) {
         ap.pts = P.pts;
         ap.pts_pitch = P.pts_pitch;
         for (int i = 0; i < 16; ++i)
             ap.q[i] = P.q[i];
-        return P.sub ? launch_agree_subpixel(ap, P.dbl, st) : launch_agree(ap, P.dbl, st);
     }
     cudaError_t e = enqueue_agree_form(P, m, ap, model, st);
-    if (e == cudaSuccess && P.pts)
+    if (e == cudaSuccess && P.pts && !fused)
         e = reproject_after(P, st);
     return e;
 }
@@ -451,6 +453,10 @@ cudaError_t bicos_gb300::enqueue_agree_form(const MatchPlan& P, const MatchBuffe
         mp.step = ap.step;
         mp.has_minvar = ap.has_minvar;
         mp.minvar = ap.minvar;
+        mp.pts = ap.pts;
+        mp.pts_pitch = ap.pts_pitch;
+        for (int i = 0; i < 16; ++i)
+            mp.q[i] = ap.q[i];
         return launch_moments(mp, P.sub ? 1 : 0, P.dbl, st);
     }
     if (P.learned)

@@ -83,6 +83,11 @@ struct MomentParams {
     float step;
     int has_minvar;
     float minvar;
+    // optional point cloud written in the same pass (modes 0 and 1), as in
+    // AgreeParams; null when unused
+    float* pts;
+    long long pts_pitch;
+    float q[16];
 };
 
 // mode 0: agree at the integer disparity, 1: subpixel sweep, 2: features

@@ -324,6 +324,9 @@ __global__ void __launch_bounds__(kRowsM) k_moments(const __grid_constant__ Mome
             reinterpret_cast<int16_t*>(reinterpret_cast<char*>(p.out) + row * p.out_pitch)[col] = out;
             if (p.corr)
                 reinterpret_cast<R*>(reinterpret_cast<char*>(p.corr) + row * p.corr_pitch)[col] = corr;
+            if (p.pts)
+                reproject_store(p.q, reinterpret_cast<float*>(reinterpret_cast<char*>(p.pts) + row * p.pts_pitch),
+                                col, row, (float)out);
         }
     } else if constexpr (MODE == 1) {
         if (in) {
@@ -465,6 +468,9 @@ __global__ void __launch_bounds__(kRowsM) k_moments(const __grid_constant__ Mome
             reinterpret_cast<float*>(reinterpret_cast<char*>(p.out) + row * p.out_pitch)[col] = result;
             if (p.corr)
                 reinterpret_cast<R*>(reinterpret_cast<char*>(p.corr) + row * p.corr_pitch)[col] = corr;
+            if (p.pts)
+                reproject_store(p.q, reinterpret_cast<float*>(reinterpret_cast<char*>(p.pts) + row * p.pts_pitch),
+                                col, row, result);
         }
     } else {
         // features: rho at col1-2..col1+2 (NaN outside the image), the left

@@ -3,7 +3,8 @@
 228-250).  The disparity and corrmap equal bicos_match_v1's bit for bit, and
 the points equal the separate reprojection pass (bicos_reproject_v1) of
 that disparity bit for bit, whether the agreement kernel wrote them
-(reference form with a threshold) or the pass ran after the match."""
+(reference and moment forms with a threshold) or the pass ran after the
+match."""
 import numpy as np
 import pytest
 
@@ -37,7 +38,9 @@ def cfg(thr=0.9, step=None, double=False, form=0, cons=None):
     (0.9, 0.1, False, 0, None),        # fused: single-precision sweep
     (0.9, 0.25, True, 0, (1, False)),  # fused: double-precision sweep
     (None, None, False, 0, None),      # no agreement stage: pass after the search
-    (0.9, 0.1, True, 1, None),         # moment form: pass after the match
+    (0.9, None, False, 1, None),       # fused: moment form, integer disparity
+    (0.9, 0.1, False, 1, (1, False)),  # fused: moment form, single-precision sweep
+    (0.9, 0.1, True, 1, None),         # fused: moment form, double-precision sweep
     (0.9, 0.1, False, 2, None),        # learned form: pass after the match
 ])
 def test_points_equal_separate_reprojection(cuda, bits, thr, step, double, form, cons):
