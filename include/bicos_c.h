@@ -246,10 +246,10 @@ bicos_status bicos_reproject_v1(const bicos_image* disparity, const double* q, b
  * the match bicos-cli runs followed by its cv::reprojectImageTo3D step
  * (src/cli.cpp:188-194, 228-250).  Arguments and outputs as
  * bicos_match_v1; q and points as bicos_reproject_v1, whose points this
- * writes bit for bit.  With a threshold, in the REFERENCE and MOMENTS
- * forms, the agreement kernel writes each pixel's point as it writes its
- * disparity (no second pass over HBM); without a threshold, or in the
- * LEARNED form, the reprojection pass runs after the match on `stream`.
+ * writes bit for bit.  With a threshold, the agreement kernels (of every
+ * NCC form) write each pixel's point as they write its disparity (no
+ * second pass over HBM); without one, the reprojection pass runs after the
+ * search on `stream`.
  */
 bicos_status bicos_match_points_v1(const bicos_image* stack0, const bicos_image* stack1, uint32_t n,
                                    bicos_image* disparity, bicos_image* corrmap, const bicos_config* cfg,

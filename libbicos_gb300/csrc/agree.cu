@@ -290,9 +290,10 @@ __global__ void __launch_bounds__(kListThreads) k_subpixel_list(const __grid_con
         }
         if (lane == 0) {
             const float bx = bk >= 0 ? xs[bk] : 0.f;
-            reinterpret_cast<float*>(reinterpret_cast<char*>(p.out) + row * p.out_pitch)[col] =
-                !(best < (TP)p.thr) ? __fsub_rn((float)d, bx) : NAN;
+            const float result = !(best < (TP)p.thr) ? __fsub_rn((float)d, bx) : NAN;
+            reinterpret_cast<float*>(reinterpret_cast<char*>(p.out) + row * p.out_pitch)[col] = result;
             put_corr<TP>(p, row, col, best);
+            agree_point(p, row, col, result);
         }
     }
 }

@@ -422,19 +422,16 @@ cudaError_t bicos_gb300::enqueue_agree(const MatchPlan& P, const MatchBuffers& m
     if (!P.thr)
         return P.pts ? reproject_after(P, st) : cudaSuccess;
     AgreeParams ap = agree_params(P, m);
-    // the reference and moment forms' kernels write the points themselves;
-    // the learned form's sweep list rewrites pixels after its first kernel
-    const bool fused = P.pts && !P.learned;
-    if (fused) {
+    // every form's agreement kernels write the points of the pixels they
+    // finish (the learned form: accepted proposals in k_learned, the rest in
+    // the sweep over its list)
+    if (P.pts) {
         ap.pts = P.pts;
         ap.pts_pitch = P.pts_pitch;
         for (int i = 0; i < 16; ++i)
             ap.q[i] = P.q[i];
     }
-    cudaError_t e = enqueue_agree_form(P, m, ap, model, st);
-    if (e == cudaSuccess && P.pts && !fused)
-        e = reproject_after(P, st);
-    return e;
+    return enqueue_agree_form(P, m, ap, model, st);
 }
 
 cudaError_t bicos_gb300::enqueue_agree_form(const MatchPlan& P, const MatchBuffers& m, const AgreeParams& ap,

@@ -889,6 +889,7 @@ __global__ void __launch_bounds__(kRowsPT) k_learned(const __grid_constant__ Lea
             reinterpret_cast<float*>(reinterpret_cast<char*>(p.out) + row * p.out_pitch)[col] = result;
             if (p.corr)
                 reinterpret_cast<TP*>(reinterpret_cast<char*>(p.corr) + row * p.corr_pitch)[col] = corr;
+            agree_point(p, row, col, result);
         }
     }
     infer_teardown(S);

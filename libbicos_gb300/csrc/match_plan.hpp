@@ -59,8 +59,8 @@ AgreeParams agree_params(const MatchPlan& plan, const MatchBuffers& m);
 // the agreement stage in the plan's form (model: the learned form's device
 // model, else unused)
 cudaError_t enqueue_agree(const MatchPlan& plan, const MatchBuffers& m, const float* model, cudaStream_t st);
-// the agreement kernels of the plan's form; ap.pts set (reference and
-// moment forms) has them write the point cloud in the same pass
+// the agreement kernels of the plan's form; ap.pts set has them write the
+// point cloud in the same pass
 cudaError_t enqueue_agree_form(const MatchPlan& plan, const MatchBuffers& m, const AgreeParams& ap,
                                const float* model, cudaStream_t st);
 

@@ -2,9 +2,8 @@
 (bicos-cli's match followed by cv::reprojectImageTo3D, src/cli.cpp:188-194,
 228-250).  The disparity and corrmap equal bicos_match_v1's bit for bit, and
 the points equal the separate reprojection pass (bicos_reproject_v1) of
-that disparity bit for bit, whether the agreement kernel wrote them
-(reference and moment forms with a threshold) or the pass ran after the
-match."""
+that disparity bit for bit, whether the agreement kernels wrote them
+(every NCC form, with a threshold) or the pass ran after the search."""
 import numpy as np
 import pytest
 
@@ -41,7 +40,8 @@ def cfg(thr=0.9, step=None, double=False, form=0, cons=None):
     (0.9, None, False, 1, None),       # fused: moment form, integer disparity
     (0.9, 0.1, False, 1, (1, False)),  # fused: moment form, single-precision sweep
     (0.9, 0.1, True, 1, None),         # fused: moment form, double-precision sweep
-    (0.9, 0.1, False, 2, None),        # learned form: pass after the match
+    (0.9, 0.1, False, 2, None),        # fused: learned form (proposals and the list's sweep)
+    (0.9, 0.1, True, 2, (1, False)),   # fused: learned form, double precision
 ])
 def test_points_equal_separate_reprojection(cuda, bits, thr, step, double, form, cons):
     sc = scenes.make_scene(60, 300, 12, seed=bits + form, bits=bits)
