@@ -193,6 +193,22 @@ def peaks():
         return 6800.0, 1900.0, "fallback"
 
 
+# FP8 tensor-core rates of this GPU (TFLOP/s by MMA N: 128 the search's
+# shape, 256 the largest single-CTA shape), measured once per run by
+# bicos_tc_fp8_rate_v1 before any timed region; empty when not measured
+FP8_RATE = {}
+
+
+def measure_fp8_rate(lbg):
+    for nn in (128, 256):
+        try:
+            FP8_RATE[nn] = round(lbg.tc_fp8_rate(nn), 1)
+        except Exception as e:  # the roofline then falls back to 2 x bf16
+            print(f"bench: FP8 rate probe (N={nn}) failed: {e}", file=sys.stderr)
+            FP8_RATE.clear()
+            return
+
+
 def profile_traffic(kernel):
     """DRAM bytes per launch of `kernel` from the committed ncu summaries
     (a line "traffic_bytes_per_launch <kernel>: <bytes>")."""
@@ -228,7 +244,10 @@ def stage_rooflines(stages, rows, cols, n, clk, valid=0.806, eb=1, nwords=4, dir
                dirs*rows*128*ceil(cols/128)*32*nwords
     search:    tensor, 2*rows*cols^2*32*nwords FLOP per direction (+-1 FP8
                dot products over the padded descriptor width) against the
-               FP8 dense rate taken as twice the measured bf16 GEMM rate
+               FP8 rate measured on this GPU (tcgen05.mma kind::f8f6f4,
+               M=128 N=256 K=32 issued alone), with the rate of the search's
+               own N=128 shape beside it; twice the measured bf16 GEMM rate
+               when the probe did not run
     agreement: HBM, bytes 2*px*n*eb (stack in) + px*(2 or 4) disparity
                out + px*(4 or 8) corrmap out (+ px*2 raw disparity in);
                the single-precision sweep's FP32 view (12 flops per valid
@@ -255,7 +274,12 @@ def stage_rooflines(stages, rows, cols, n, clk, valid=0.806, eb=1, nwords=4, dir
     sweep = agree.startswith("subpixel") or agree == "moments"
     ag_bytes = 2 * px * n * eb + px * (4 if sweep else 2) + px * (8 if dbl else 4) + px * 2
     fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
-    fp8_peak = 2 * bf16
+    if FP8_RATE:
+        fp8_peak = FP8_RATE[256]
+        fp8_src = "measured FP8 tcgen05.mma rate, M128 N256 K32 issued alone (bicos_tc_fp8_rate_v1)"
+    else:
+        fp8_peak = 2 * bf16
+        fp8_src = f"FP8 dense = 2 x {src} bf16 GEMM rate"
     tf_kernel = "k_transform_full" if full else "k_transform_limited"
     ag_kernel = {"subpixel_f32": "k_subpixel_f32", "subpixel_f64": "k_subpixel_f64", "agree": "k_agree",
                  "moments": "k_moments"}[agree]
@@ -270,7 +294,7 @@ def stage_rooflines(stages, rows, cols, n, clk, valid=0.806, eb=1, nwords=4, dir
         "search": {"kernel": "k_search_tc", "bound": "tensor", "ms": round(t_se, 4),
                    "achieved": round(se_flop / (t_se * 1e-3) / 1e12, 1), "peak": round(fp8_peak, 1),
                    "unit": "TFLOP/s", "frac": round(se_flop / (t_se * 1e-3) / 1e12 / fp8_peak, 4),
-                   "peak_source": f"FP8 dense = 2 x {src} bf16 GEMM rate",
+                   "peak_source": fp8_src,
                    "traffic": profile_traffic("k_search_tc"), "algorithmic_flop": se_flop,
                    "directions": dirs},
         "agreement": {"kernel": ag_kernel, "bound": "hbm", "ms": round(t_ag, 4),
@@ -278,6 +302,11 @@ def stage_rooflines(stages, rows, cols, n, clk, valid=0.806, eb=1, nwords=4, dir
                       "frac": round(gbs(ag_bytes, t_ag) / hbm, 4), "peak_source": f"{src} HBM copy bandwidth",
                       "traffic": profile_traffic(ag_kernel), "algorithmic_bytes": ag_bytes},
     }
+    if FP8_RATE:
+        se = out["search"]
+        se["shape_peak"] = FP8_RATE[128]
+        se["frac_of_shape_peak"] = round(se["achieved"] / FP8_RATE[128], 4)
+        se["peak_2x_bf16"] = round(2 * bf16, 1)
     if agree == "subpixel_f32":
         ag_flop = 12.0 * valid * px * positions * n
         out["agreement"]["fp32"] = {
@@ -456,6 +485,7 @@ def run_ours(args):
 
     B.build()
     L = lbg.load_library()
+    measure_fp8_rate(lbg)
     scene = scenes.workload_scene(WORKLOAD, seed=args.seed + rank)
     n, rows, cols = scene.left.shape
     px = rows * cols
@@ -527,9 +557,9 @@ def run_ours(args):
     }
     result["stage_ms"] = {"transform": round(stages[0], 4), "search": round(stages[1], 4),
                           "agreement": round(stages[2], 4)}
-    # per step: the descriptor transform, the FP8 expansion of the candidate
-    # descriptors, the tensor-core search, the subpixel sweep
-    result["gpu_launches"] = 4 * args.steps
+    # per step: the descriptor transform (which also writes the search's FP8
+    # candidate tiles), the tensor-core search, the subpixel sweep
+    result["gpu_launches"] = 3 * args.steps
 
     # per-stage rooflines; the headline one is the stage that takes longest
     result["stage_rooflines"] = stage_rooflines(stages, rows, cols, n, clk, valid)
@@ -566,7 +596,9 @@ def run_ours(args):
             "stage_ms": {"transform": round(st_l[0], 4), "search": round(st_l[1], 4),
                          "agree_learned": round(st_l[2], 4)},
             "agree_stage_vs_plain_sweep": round(stages[2] / st_l[2], 3),
-            "gpu_launches_per_step": 7,
+            # transform, search, sweep offsets, k_learned, the list's sweep
+            # (and one cudaMemsetAsync of the list's counters)
+            "gpu_launches_per_step": 5,
             "error": learned_error(lbg, pybicos, left, right, out[0], out_l[0], n)}
 
     if not args.no_batch and ws == 1:

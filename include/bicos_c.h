@@ -415,6 +415,18 @@ int32_t bicos_batch_captures(const bicos_batch* batch);
 bicos_status bicos_stage_timing(int32_t enable);
 bicos_status bicos_stage_times(float* ms_per_stage /* [3] */, int32_t* calls);
 
+/*
+ * FP8 tensor-core rate of the current device for the Hamming search's MMA
+ * shape, a measurement tool with no counterpart in the reference: the
+ * instruction stream of the search (tcgen05.mma kind::f8f6f4, M = 128,
+ * K = 32, four per 128-bit tile) issued alone, two CTAs per SM, timed with
+ * CUDA events over three launches.  n = 128 is the search's shape, n = 256
+ * the largest single-CTA shape.  *tflops receives 2 x M x N x K per
+ * instruction over the time.  Synchronises its own stream; call it when
+ * nothing else runs on the device.
+ */
+bicos_status bicos_tc_fp8_rate_v1(int32_t n, double* tflops);
+
 /* Number of kernel blocks on this device whose bounded waits ran out since
  * load (0 in normal operation; such a block records the event instead of
  * hanging and leaves its outputs unwritten).  Synchronises the device. */

@@ -19,7 +19,7 @@ from .pybicos import Config, Precision, TransformMode, Variant
 
 __all__ = ["pybicos", "Config", "Precision", "TransformMode", "Variant", "match_device",
            "descriptor_transform", "search", "agree", "agree_subpixel", "descriptor_words",
-           "subpixel_features", "agree_learned", "Batch",
+           "subpixel_features", "agree_learned", "Batch", "tc_fp8_rate",
            "load_library", "required_bits"]
 
 
@@ -165,6 +165,17 @@ def reproject(disparity, q, out=None, stream=None):
     _raise(N.load().bicos_reproject_v1(C.byref(di), qa.ctypes.data_as(C.POINTER(C.c_double)), C.byref(pi),
                                        _stream_ptr(stream)))
     return out
+
+
+def tc_fp8_rate(n: int = 128) -> float:
+    """FP8 tensor-core rate of the current device in TFLOP/s for the
+    search's MMA shape (bicos_tc_fp8_rate_v1): n = 128 the search's
+    M = 128 x N = 128 x K = 32 instructions issued alone, n = 256 the
+    largest single-CTA shape.  A measurement tool, the denominator of the
+    search's roofline."""
+    v = C.c_double()
+    _raise(N.load().bicos_tc_fp8_rate_v1(int(n), C.byref(v)))
+    return v.value
 
 
 def agree(disp, stack0, stack1, threshold: float, min_var=None, double=False, stream=None):

@@ -83,6 +83,7 @@ def load():
         "bicos_release_scratch": ([], C.c_int),
         "bicos_stage_timing": ([I], C.c_int),
         "bicos_kernel_faults": ([], I),
+        "bicos_tc_fp8_rate_v1": ([I, C.POINTER(C.c_double)], C.c_int),
         "bicos_stage_times": ([C.POINTER(C.c_float), C.POINTER(I)], C.c_int),
         "bicos_descriptor_transform_v1": ([IMG, U, I, U, P, P], C.c_int),
         "bicos_search_v1": ([P, P, I, I, U, I, I, IMG, P], C.c_int),

@@ -105,6 +105,16 @@ def test_no_kernel_wait_ran_out(cuda, native):
     assert native.load().bicos_kernel_faults() == 0
 
 
+def test_fp8_rate_probe(cuda, native):
+    """bicos_tc_fp8_rate_v1: the search's MMA stream alone gives a finite
+    positive rate, the N = 256 shape no less than 0.8 of it, and no
+    completion wait runs out"""
+    r128, r256 = lbg.tc_fp8_rate(128), lbg.tc_fp8_rate(256)
+    assert 0.0 < r128 < 20000.0 and 0.0 < r256 < 20000.0
+    assert r256 > 0.8 * r128
+    assert native.load().bicos_kernel_faults() == 0
+
+
 def test_search_known_answers(cuda):
     """the hand-worked cases of tests/test_oracle_kat.py on the GPU, in the
     plain and the column-coded form"""

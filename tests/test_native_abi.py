@@ -128,6 +128,17 @@ def test_points_entry_checks_before_any_device_work(native):
     assert lib.bicos_last_error() == b"Q must be finite"
 
 
+def test_tc_rate_argument_checks(native):
+    """the FP8 rate probe refuses shapes other than N = 128 / 256 before any
+    device work"""
+    lib = native.load()
+    v = C.c_double()
+    for n in (0, 64, 192, 512):
+        assert lib.bicos_tc_fp8_rate_v1(n, C.byref(v)) == native.ERR_INVALID_ARGUMENT
+    assert lib.bicos_tc_fp8_rate_v1(128, None) == native.ERR_INVALID_ARGUMENT
+    assert b"n must be 128 or 256" in lib.bicos_last_error()
+
+
 def test_version(native):
     assert b"sm_103a" in native.load().bicos_version()
 
