@@ -1,4 +1,4 @@
-// Persistent multi-stack launches (the batch API, batch.cu).
+// Persistent multi-stack launches (the batch API, batch_api.cu).
 //
 // A kernel that normally runs as a grid over one stack is written as a
 // block body taking virtual block coordinates (bx, by, bz).  k_batch runs

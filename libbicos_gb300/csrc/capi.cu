@@ -499,7 +499,7 @@ int32_t bicos_descriptor_words(uint32_t n, int32_t mode, int32_t max_bits) {
 }
 
 int32_t bicos_kernel_faults(void) {
-    return (int32_t)(read_tc_faults() + read_moment_faults() + read_mlp_faults());
+    return (int32_t)(read_tc_faults() + read_moment_faults() + read_mlp_faults() + read_rate_faults());
 }
 
 bicos_status bicos_stage_timing(int32_t enable) {

@@ -1,5 +1,6 @@
-// Internal interface between the host orchestration (capi.cu) and the
-// sm_103a kernels (transform.cu, search.cu, agree.cu).
+// Internal interface between the host orchestration (capi.cu, batch_api.cu)
+// and the sm_103a kernels (transform.cu, search_tc.cu, search.cu, agree.cu,
+// moments.cu, learned.cu, reproject.cu, mma_rate.cu).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -101,7 +102,6 @@ unsigned int read_moment_faults();
 cudaError_t launch_transform(const StackParams& p, int sides, bool full, int nwords,
                              uint32_t* desc0, uint32_t* desc1, cudaStream_t st, uint8_t* tiles0 = nullptr,
                              uint8_t* tiles1 = nullptr, int bits = 0);
-// number of transform CTAs whose bulk-copy wait ran out (synchronous)
 
 // Row-wise arg-min.  When disp != nullptr (one direction, NODUPES or plain)
 // the kernel writes int16 disparities col0 - best directly; otherwise it
@@ -140,6 +140,8 @@ cudaError_t launch_search_tc(const uint32_t* desc0, const uint32_t* desc1, int r
                              bool xbuf_ready = false);
 // number of tensor-core search CTAs whose bounded waits ran out (synchronous)
 unsigned int read_tc_faults();
+// the same for the FP8 rate probe (mma_rate.cu)
+unsigned int read_rate_faults();
 
 cudaError_t launch_consistency(const int32_t* fwd, const int32_t* rev, int rows, int cols,
                                int max_lr_diff, int16_t* disp, long long disp_pitch,
@@ -184,8 +186,9 @@ unsigned int read_mlp_faults();
 // message when none is installed)
 const float* learned_model_device(cudaStream_t st, std::string* err);
 
-// batch API (batch.cu): all jobs of one kernel class in one persistent
-// launch over a work table (batch.cuh: BatchWork, BatchLaunch)
+// batch API (batch_api.cu; the kernels in transform.cu and agree.cu): all
+// jobs of one kernel class in one persistent launch over a work table
+// (batch.cuh: BatchWork, BatchLaunch)
 template<typename P>
 struct BatchArgs;
 struct BatchLaunch;

@@ -14,7 +14,7 @@
 // TMEM columns: N = 128 alternates two 128-column accumulators as the
 // search does, N = 256 accumulates into one.  The completion wait is
 // bounded; a CTA whose wait runs out counts itself in g_rate_faults, which
-// the entry point turns into an error.
+// the entry point turns into an error (and bicos_kernel_faults counts).
 #include <cuda_runtime.h>
 
 #include <string>
@@ -24,6 +24,15 @@
 #include "tcgen05.cuh"
 
 namespace bicos_gb300 {
+
+__device__ unsigned int g_rate_faults = 0;
+
+unsigned int read_rate_faults() {
+    unsigned int v = 0;
+    cudaMemcpyFromSymbol(&v, g_rate_faults, sizeof v);
+    return v;
+}
+
 namespace {
 
 using namespace tc;
@@ -34,8 +43,6 @@ constexpr int kRateK = 128;  // bytes of K per round: the search's 128-bit descr
 // CTA (and no third TMEM allocation) lands on an SM
 constexpr int kRateSmem = 100 * 1024;
 constexpr int kRateLaunches = 3;
-
-__device__ unsigned int g_rate_faults = 0;
 
 template<int N>
 __global__ void __launch_bounds__(kRateThreads, 2) k_fp8_mma_rate(int rounds) {
@@ -91,12 +98,6 @@ __global__ void __launch_bounds__(kRateThreads, 2) k_fp8_mma_rate(int rounds) {
     fence_after();
     if (warp == 0)
         tmem_dealloc(tmem, 256);
-}
-
-unsigned int read_rate_faults() {
-    unsigned int v = 0;
-    cudaMemcpyFromSymbol(&v, g_rate_faults, sizeof v);
-    return v;
 }
 
 template<int N>
